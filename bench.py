@@ -1,0 +1,335 @@
+#!/usr/bin/env python3
+"""Benchmark: Yee cell-updates per second on the 512 x 512 x 400 phantom.
+
+Workload: 8 nested, seeded ellipsoids of Debye tissue in vacuum (uint8 class
+volume), a 900 MHz three-cell Ez dipole 20 cells outside the outer shell,
+Mur faces, dx = 1 mm, reference scheme, FP32 fields.  One step is one full
+Yee step (H, D + sources, Debye E, Mur) over all 104,857,600 cells.  The
+state (7.6 GB) is far larger than L2, so no flush is needed between steps.
+
+Default arm (``--impl gb300``): the library's solver, steps replayed as CUDA
+graphs; per-kernel times from fdtd_solver_profile give the roofline;
+``e2e`` repeats the run through the C ABI with host buffers (material upload,
+a per-step Ez plane snapshot, final field read-back) inside the timed region.
+``--impl reference`` times the CPU implementation of the reference kernels
+(the FP32 oracle port, bit-identical to them) on all host cores.
+
+Multi-GPU (torchrun): every rank runs its own solve (replicas, weak scaling);
+value = all ranks' cell-updates / slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+B_ALG = 97  # bytes per cell-update: 15 state floats read, 9 written, 1-byte class
+METRIC = "cell-updates/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--dims", type=int, nargs=3, default=[512, 512, 400], metavar=("NX", "NY", "NZ"))
+    ap.add_argument("--kernel", choices=["single", "two_pass"], default="single")
+    ap.add_argument("--scheme", choices=["reference", "corrected"], default="reference")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------- workload
+
+def make_workload(nx: int, ny: int, nz: int, tmp: Path):
+    """Phantom codes, class table and Params read back from input_params."""
+    import fdtd_gb300 as fg
+    from fdtd_gb300 import phantom as ph
+
+    codes, mats, cfg = ph.c2_config((nz, ny, nx))
+    cfg.env_dir = str(tmp / "pgm")
+    cfg.output_dir = str(tmp / "out")
+    ph.write_input_params(tmp / "input_params", cfg)
+    ph.write_mat_specs(tmp / "mat_specs", mats)
+    p = fg.Params.read(tmp / "input_params")
+    specs = fg.read_specs(tmp / "mat_specs")[: len(mats)]
+    return p, codes, specs
+
+
+def workload_config(args, p) -> dict:
+    nx, ny, nz = args.dims
+    return {"workload": f"nested-ellipsoid Debye phantom {nx}x{ny}x{nz}, 8 tissue classes + vacuum, "
+                        f"900 MHz 3-cell Ez dipole, Mur ABC, dx=1 mm",
+            "nx": nx, "ny": ny, "nz": nz, "cells": nx * ny * nz, "scheme": args.scheme, "kernel": args.kernel,
+            "sources": [list(s) for s in p.sources], "dt_s": float(p.dt),
+            "l2": "state 7.6 GB >> 129 MB L2: inputs larger than L2, no flush",
+            "b_alg_bytes_per_cell_update": B_ALG}
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.out = None
+
+    def __enter__(self):
+        try:
+            self.out = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if self.proc is None or self.out is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.out.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.out.read())) if len(r) >= 9]
+        sm, mx, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+                power.append(float(r[3]))
+            except ValueError:
+                continue
+            for k, n in enumerate(names):
+                if r[5 + k].strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def measured_peak_gbs() -> tuple[float, str]:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        try:
+            return float(json.loads(f.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def committed_traffic(kernel: str, cells: int):
+    """DRAM bytes per launch from the committed ncu summary, scaled to cells."""
+    f = ROOT / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    try:
+        rec = json.loads(f.read_text())[kernel]
+        return float(rec["dram_bytes_per_cell"]) * cells
+    except (KeyError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------- CPU arms
+
+def cpu_port_rate(p, codes, specs, seconds: float, nthreads: int, max_steps: int | None = None):
+    """Cell-updates/s of the FP32 oracle port (bit-identical to the reference
+    kernels run on a CPU) on a z-slab of the workload."""
+    from oracle import pyoracle as po
+
+    nx, ny = p.nx, p.ny
+    sz = 8
+    srcz = p.sources[0][2] if p.sources else p.nz // 2
+    z0 = max(0, min(p.nz - sz, srcz - sz // 2))
+    slab = np.ascontiguousarray(codes[z0:z0 + sz])
+    media = po.Media(*(np.ascontiguousarray(specs[slab, k]) for k in (0, 2, 1, 3)))
+    media.rp = [np.ones(s, np.float32) for s in po.rp_shapes(nx, ny, sz)]
+    jz = p.setup_sources()
+    srcs = [(x, y, z - z0) for (x, y, z) in p.sources if z0 <= z < z0 + sz]
+    consts = dict(dt=p.dt, dx=p.dx, dy=p.dy, dz=p.dz, mu0=p.mu0, eps0=p.eps0)
+    cfg = po.make_cfg((nx, ny, sz), jz, sources=srcs, consts=consts, nthreads=nthreads)
+    st = po.State(nx, ny, sz, np.float32)
+    po.run(cfg, media, st, 0, 1)  # warm-up
+    done, t0 = 0, time.perf_counter()
+    while True:
+        po.run(cfg, media, st, 1 + done, 1)
+        done += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or (max_steps is not None and done >= max_steps):
+            break
+    cells = nx * ny * sz
+    return cells * done / el, f"{nx}x{ny}x{sz} z-slab of the workload, {done} steps, FP32 port of the reference kernels"
+
+
+# ------------------------------------------------------------------- arms
+
+def run_reference_arm(args, rank: int, world: int) -> None:
+    if rank != 0:
+        return
+    with tempfile.TemporaryDirectory() as tmp:
+        nx, ny, nz = args.dims
+        p, codes, specs = make_workload(nx, ny, nz, Path(tmp))
+        threads = os.cpu_count() or 1
+        budget = max(10.0, min(120.0, args.cpu_seconds * 4))
+        rate, sample = cpu_port_rate(p, codes, specs, budget, threads, max_steps=args.steps)
+        cfg = workload_config(args, p)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": nx * ny * nz / rate * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": cfg,
+            "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
+    import torch
+
+    import fdtd_gb300 as fg
+    from fdtd_gb300 import replicas
+
+    torch.cuda.set_device(local_rank)
+    nx, ny, nz = args.dims
+    cells = nx * ny * nz
+    kernel = fg.KERNEL_SINGLE_PASS if args.kernel == "single" else fg.KERNEL_TWO_PASS
+    scheme = fg.SCHEME_REFERENCE if args.scheme == "reference" else fg.SCHEME_CORRECTED
+    tmp = tempfile.TemporaryDirectory()
+    p, codes, specs = make_workload(nx, ny, nz, Path(tmp.name))
+
+    # ---- device-resident throughput (value)
+    s = fg.Solver(p, codes, specs, scheme=scheme, kernel=kernel, device=local_rank)
+    stream = torch.cuda.ExternalStream(s.stream)
+    s.run(args.warmup)
+    s.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        replicas.barrier(dist)
+        torch.cuda.synchronize()
+        start.record(stream)
+        s.run(args.steps)
+        end.record(stream)
+        s.synchronize()
+        torch.cuda.synchronize()
+        replicas.barrier(dist)
+    seconds = start.elapsed_time(end) / 1e3
+    total_cells, tmax = replicas.aggregate(cells * args.steps, seconds, dist, device=f"cuda:{local_rank}")
+    clocks = clk.summary()
+    prof = s.profile(min(args.steps, 20))
+    kernels_per_step = len(prof)
+    s.close()
+
+    # ---- end to end through the C ABI with host buffers (e2e)
+    e2e = None
+    if not args.no_e2e:
+        srcz = p.sources[0][2] if p.sources else nz // 2
+        plane_bytes = 4 * nx * ny
+        got = []
+        torch.cuda.synchronize()
+        replicas.barrier(dist)
+        t0 = time.perf_counter()
+        s2 = fg.Solver(p, codes, specs, scheme=scheme, kernel=kernel, device=local_rank)
+        s2.set_snapshots(every=1, fields=("ez",), z0=srcz, nplanes=1, callback=lambda st, n, a: got.append(st))
+        s2.run(args.steps)
+        s2.flush_snapshots()
+        final = s2.field("ez")
+        t1 = time.perf_counter()
+        s2.close()
+        replicas.barrier(dist)
+        assert len(got) == args.steps and final.shape == (nz, ny, nx)
+        h2d = codes.nbytes + 4 * (len(specs) * 8 + 65536 + 2 * (2 * ny * nz + 2 * nx * nz + 2 * nx * ny))
+        d2h = plane_bytes * args.steps + final.nbytes
+        e_cells, e_t = replicas.aggregate(cells * args.steps, t1 - t0, dist, device=f"cuda:{local_rank}")
+        e2e = {"value": e_cells / e_t, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / args.steps,
+               "d2h_bytes_per_step": d2h / args.steps,
+               "includes": "solver create (material + plan upload), per-step Ez plane D2H through the pinned "
+                           "snapshot ring, final Ez volume read-back, destroy"}
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, sample = cpu_port_rate(p, codes, specs, args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port", "sample": sample}
+    tmp.cleanup()
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak_gbs()
+    main = "fused_step" if "fused_step" in prof else max(prof, key=prof.get)
+    main_ms = prof[main]
+    achieved = B_ALG * cells / (main_ms / 1e3) / 1e9
+    step_ms = sum(prof.values())
+    line = {
+        "metric": METRIC, "value": total_cells / tmax, "unit": "cell-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(args, p),
+        "roofline": {"bound": "hbm", "kernel": main, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": committed_traffic(main, cells),
+                     "algorithmic_bytes_per_launch": B_ALG * cells, "avg_launch_ms": main_ms,
+                     "step_hbm_frac": B_ALG * cells / (step_ms / 1e3) / 1e9 / peak},
+        "kernel_ms": prof,
+        "gpu_launches": kernels_per_step * args.steps,
+        "clocks": clocks,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main() -> None:
+    args = parse_args()
+    from fdtd_gb300 import replicas
+
+    rank, local_rank, world = replicas.dist_env()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as td
+
+        if args.impl == "gb300":
+            torch.cuda.set_device(local_rank)
+        td.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+        dist = td
+    try:
+        if args.impl == "reference":
+            run_reference_arm(args, rank, world)
+        else:
+            run_gb300_arm(args, rank, local_rank, world, dist)
+    finally:
+        if dist is not None:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

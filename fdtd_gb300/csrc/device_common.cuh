@@ -1,0 +1,140 @@
+// device_common.cuh -- device helpers shared by the compat and native kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fdtd_internal.h"
+
+namespace fdtd {
+
+__host__ __device__ inline size_t cell_index(int x, int y, int z, int nx, int ny)
+{
+    return ((size_t)z * (size_t)ny + (size_t)y) * (size_t)nx + (size_t)x;
+}
+
+// Debye E update of one component (fdtd_calculations.cu:150-156): E^{n+1} =
+// c (d E^n - a E^{n-1} + k1 D^{n+1} - k2 D^n + k3 D^{n-1}), the D terms in
+// the difference form of DebyeCoef.
+__device__ __forceinline__ float debye_update(const DebyeCoef &k, float e0, float e1, float d0, float d1, float d2)
+{
+    const float p = k.d * e0 - k.a * e1;
+    const float g1 = d0 - d1;
+    const float g2 = d1 - d2;
+    const float q = k.two_dt * g1 + k.two_tau * (g1 - g2) + k.delta * d0;
+    return k.c * (p + q);
+}
+
+// The reference's per-cell coefficients (fdtd_calculations.cu:141-144) in
+// single precision.  The reference evaluates a, b, c, d with double literals;
+// here c is the correctly rounded reciprocal of the same float sum, d is the
+// same single rounding, a and b may differ from it by one unit in the last
+// place.  delta comes from an exact two-sum of dt + tau.
+__device__ __forceinline__ DebyeCoef cell_coef(float dt, float eps0, float sigma, float eps_s, float eps_i, float tau,
+                                               int scheme)
+{
+    DebyeCoef k;
+    const float a = 2.0f * eps0 * eps_i * tau;
+    const float b = a + 2.0f * dt * (eps0 * eps_s + sigma * tau);
+    const float s = __fmul_rn(__fmul_rn(sigma, dt), dt);
+    k.a = a;
+    k.c = __frcp_rn(__fadd_rn(b, s));
+    k.d = scheme == FDTD_SCHEME_CORRECTED ? __fsub_rn(__fadd_rn(a, b), s) : __fsub_rn(2.0f * b, s);
+    k.two_dt = 2.0f * dt;
+    k.two_tau = 2.0f * tau;
+    const float sum = __fadd_rn(dt, tau);
+    const float bb = __fsub_rn(sum, dt);
+    const float err = __fadd_rn(__fsub_rn(dt, __fsub_rn(sum, bb)), __fsub_rn(tau, bb));
+    k.delta = -2.0f * err;
+    k.pad0 = k.pad1 = 0.0f;
+    return k;
+}
+
+// First-order Mur value of one face cell (fdtd_calculations.cu:240-248 and
+// mirrors).  rp_self is the slab layer on the face, rp_nbr one cell inwards;
+// t_nbr is E^{n+1} at the inner neighbour, s_nbr and s_self are E^n.
+__device__ __forceinline__ float mur_value(float dt, float h, float me, float rp_self, float rp_nbr, float t_nbr,
+                                           float s_nbr, float s_self)
+{
+    const float q_self = h * sqrtf(me * rp_self);
+    const float q_nbr = h * sqrtf(me * rp_nbr);
+    return 1.0f / (dt + q_self) * ((dt - q_nbr) * t_nbr + (dt + q_nbr) * s_nbr - (dt - q_self) * s_self);
+}
+
+// The twelve (component, face) sets that updateMurBoundary writes.  For face
+// set f, (len_u, len_v) is the extent and (u0, v0) the first coordinate of
+// its two in-face axes; `axis` is the face normal (0 x, 1 y, 2 z) and `far`
+// selects the face at n-1.
+struct MurFace {
+    int comp, axis, far;
+    int u0, len_u, v0, len_v;  // u is the faster in-face axis (x, else y)
+};
+
+__host__ __device__ inline MurFace mur_face(int f, int nx, int ny, int nz)
+{
+    MurFace m;
+    m.comp = f / 4;
+    m.far = f & 1;
+    const int pair = (f >> 1) & 1;
+    if (m.comp == 0) {          // ex: y faces (x 0..nx-2, z 1..nz-2), z faces (x 0..nx-2, y 1..ny-2)
+        m.axis = pair ? 2 : 1;
+        m.u0 = 0; m.len_u = nx - 1;
+        if (m.axis == 1) { m.v0 = 1; m.len_v = nz - 2; }
+        else { m.v0 = 1; m.len_v = ny - 2; }
+    } else if (m.comp == 1) {   // ey: x faces (y 0..ny-2, z 1..nz-2), z faces (x 1..nx-2, y 0..ny-2)
+        m.axis = pair ? 2 : 0;
+        if (m.axis == 0) { m.u0 = 0; m.len_u = ny - 1; m.v0 = 1; m.len_v = nz - 2; }
+        else { m.u0 = 1; m.len_u = nx - 2; m.v0 = 0; m.len_v = ny - 1; }
+    } else {                    // ez: x faces (y 1..ny-2, z 0..nz-2), y faces (x 1..nx-2, z 0..nz-2)
+        m.axis = pair ? 1 : 0;
+        if (m.axis == 0) { m.u0 = 1; m.len_u = ny - 2; m.v0 = 0; m.len_v = nz - 1; }
+        else { m.u0 = 1; m.len_u = nx - 2; m.v0 = 0; m.len_v = nz - 1; }
+    }
+    return m;
+}
+
+struct MurSlabs {
+    const float *rpx0, *rpy0, *rpz0, *rpx_end, *rpy_end, *rpz_end;
+};
+
+// Applies updateMurBoundary to face set f, in-face position (iu, iv).
+// eT: E^{n+1} (written), eS: E^n.  fix_ey selects the corrected scheme's
+// E^{n+1} term on the ey x = nx-1 face (the reference reads E^n there, :323).
+__device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny, int nz, float dt, float hx, float hy,
+                                          float hz, float me, const MurSlabs &rp, float *const eT[3],
+                                          const float *const eS[3], bool fix_ey)
+{
+    const MurFace m = mur_face(f, nx, ny, nz);
+    if (iu >= m.len_u || iv >= m.len_v)
+        return;
+    const int u = m.u0 + iu, v = m.v0 + iv;
+    int x, y, z, dxn = 0, dyn = 0, dzn = 0;
+    float h, rs, rn;
+    if (m.axis == 0) {
+        x = m.far ? nx - 1 : 0; y = u; z = v; dxn = m.far ? -1 : 1; h = hx;
+        const float *slab = m.far ? rp.rpx_end : rp.rpx0;
+        const size_t base = ((size_t)z * ny + y) * 2;
+        rs = slab[base + (m.far ? 1 : 0)];
+        rn = slab[base + (m.far ? 0 : 1)];
+    } else if (m.axis == 1) {
+        x = u; y = m.far ? ny - 1 : 0; z = v; dyn = m.far ? -1 : 1; h = hy;
+        const float *slab = m.far ? rp.rpy_end : rp.rpy0;
+        rs = slab[((size_t)z * 2 + (m.far ? 1 : 0)) * nx + x];
+        rn = slab[((size_t)z * 2 + (m.far ? 0 : 1)) * nx + x];
+    } else {
+        x = u; y = v; z = m.far ? nz - 1 : 0; dzn = m.far ? -1 : 1; h = hz;
+        const float *slab = m.far ? rp.rpz_end : rp.rpz0;
+        rs = slab[((size_t)(m.far ? 1 : 0) * ny + y) * nx + x];
+        rn = slab[((size_t)(m.far ? 0 : 1) * ny + y) * nx + x];
+    }
+    const size_t i = cell_index(x, y, z, nx, ny);
+    const size_t j = cell_index(x + dxn, y + dyn, z + dzn, nx, ny);
+    const float *S = eS[m.comp];
+    float *T = eT[m.comp];
+    // fdtd_calculations.cu:323: the ey face at x = nx-1 reads E^n at x-1 in
+    // its first term as well.
+    const bool quirk = m.comp == 1 && m.axis == 0 && m.far && !fix_ey;
+    const float t_nbr = quirk ? S[j] : T[j];
+    T[i] = mur_value(dt, h, me, rs, rn, t_nbr, S[j], S[i]);
+}
+
+}  // namespace fdtd

@@ -1,0 +1,404 @@
+// native.cu -- the native fused path: plan, H kernel, D+source+E kernel, Mur.
+//
+// State (fdtd_native_fields): H, two E slots, two D slots, a uint8 material
+// class per cell.  Step n reads E^n, D^n from the current slots and E^{n-1},
+// D^{n-1} from the "prev" slots, which receive E^{n+1}, D^{n+1} cell by cell
+// after they are read.  Every cell is either written on every step or never
+// written, so two slots reproduce the reference's three-slot rotation
+// (fdtd.cu:115-530) exactly.
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "device_common.cuh"
+#include "native.cuh"
+
+namespace fdtd {
+
+DebyeCoef debye_coef(float dt, float eps0, float sigma, float eps_s, float eps_i, float tau, int scheme)
+{
+    // updateEField's per-cell coefficients (fdtd_calculations.cu:141-144),
+    // double literals and float storage exactly as there.
+    DebyeCoef k{};
+    const float a = 2.0 * eps0 * eps_i * tau;
+    const float b = a + 2.0 * dt * (eps0 * eps_s + sigma * tau);
+    const float c = 1.0 / (b + sigma * dt * dt);
+    const float d = scheme == FDTD_SCHEME_CORRECTED ? (1.0 * a + b - sigma * dt * dt) : (2.0 * b - sigma * dt * dt);
+    k.a = a;
+    k.c = c;
+    k.d = d;
+    k.two_dt = 2.0f * dt;
+    k.two_tau = 2.0f * tau;
+    const float s = dt + tau;
+    k.delta = (float)(2.0 * ((double)s - ((double)dt + (double)tau)));
+    return k;
+}
+
+NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)
+{
+    NativeConsts c{};
+    c.nx = p->nx;
+    c.ny = p->ny;
+    c.nz = p->nz;
+    c.kx = p->dt / (p->mu0 * p->dx);
+    c.ky = p->dt / (p->mu0 * p->dy);
+    c.kz = p->dt / (p->mu0 * p->dz);
+    c.tx = p->dt / p->dx;
+    c.ty = p->dt / p->dy;
+    c.tz = p->dt / p->dz;
+    c.dt = p->dt;
+    c.hx = p->dx;
+    c.hy = p->dy;
+    c.hz = p->dz;
+    c.me = p->mu0 * p->eps0;
+    c.scheme = p->scheme;
+    c.nsources = p->nsources;
+    for (int s = 0; s < p->nsources; s++)
+        for (int k = 0; k < 3; k++)
+            c.sources[3 * s + k] = p->sources[3 * s + k];
+    c.coef = p->d_coef;
+    c.nclasses = p->nclasses;
+    c.jz = p->d_jz;
+    c.njz = p->njz;
+    c.rp = p->rp;
+    c.step = n;
+    c.step_counter = nullptr;
+    if (f) {
+        for (int k = 0; k < 3; k++) {
+            c.h_in[k] = (&f->hx)[k];
+            c.h_out[k] = (&f->hx_out)[k];
+            c.e_cur[k] = (&f->ex)[k];
+            c.e_prev[k] = (&f->ex_prev)[k];
+            c.d_cur[k] = (&f->dx)[k];
+            c.d_prev[k] = (&f->dx_prev)[k];
+        }
+        c.mat = f->material;
+    }
+    return c;
+}
+
+namespace {
+
+constexpr int TX = 32, TY = 8;
+
+__device__ __forceinline__ DebyeCoef load_coef(const DebyeCoef *__restrict__ table, int cls)
+{
+    const float4 *p = reinterpret_cast<const float4 *>(table + cls);
+    const float4 u = __ldg(p), v = __ldg(p + 1);
+    DebyeCoef k;
+    k.a = u.x; k.c = u.y; k.d = u.z; k.two_dt = u.w;
+    k.two_tau = v.x; k.delta = v.y; k.pad0 = v.z; k.pad1 = v.w;
+    return k;
+}
+
+// updateHField (fdtd_calculations.cu:32-77) with separate in and out buffers
+// (they may alias).
+__global__ void __launch_bounds__(TX *TY) native_h_kernel(NativeConsts c)
+{
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y, z = blockIdx.z;
+    if (x >= nx - 1 || y >= ny - 1 || z >= nz - 1)
+        return;  // no H component is updated at x = nx-1, y = ny-1 or z = nz-1
+    const size_t i = cell_index(x, y, z, nx, ny);
+    const size_t sx = 1, sy = nx, sz = (size_t)nx * ny;
+    const float *__restrict__ ex = c.e_cur[0];
+    const float *__restrict__ ey = c.e_cur[1];
+    const float *__restrict__ ez = c.e_cur[2];
+    const float ex0 = ex[i], ey0 = ey[i], ez0 = ez[i];
+    if (x >= 1)
+        c.h_out[0][i] = c.h_in[0][i] - c.ky * (ez[i + sy] - ez0) + c.ky * (ey[i + sz] - ey0);
+    if (y >= 1)
+        c.h_out[1][i] = c.h_in[1][i] - c.kz * (ex[i + sz] - ex0) + c.kx * (ez[i + sx] - ez0);
+    if (z >= 1)
+        c.h_out[2][i] = c.h_in[2][i] - c.kx * (ey[i + sx] - ey0) + c.ky * (ex[i + sy] - ex0);
+}
+
+__device__ __forceinline__ int source_sample_index(const NativeConsts &c, int n)
+{
+    return c.scheme == FDTD_SCHEME_CORRECTED ? n : n - n % 3;
+}
+
+// updateDField + updateSources + updateEField for one cell (fdtd_calculations.cu
+// :80-122, :187-213, :125-184).  H^{n+1/2} is read from h_out.
+__global__ void __launch_bounds__(TX *TY) native_de_kernel(NativeConsts c)
+{
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const int x = blockIdx.x * TX + threadIdx.x, y = blockIdx.y * TY + threadIdx.y, z = blockIdx.z;
+    if (x >= nx || y >= ny)
+        return;
+    const size_t i = cell_index(x, y, z, nx, ny);
+    const size_t sx = 1, sy = nx, sz = (size_t)nx * ny;
+    const float *__restrict__ hx = c.h_out[0];
+    const float *__restrict__ hy = c.h_out[1];
+    const float *__restrict__ hz = c.h_out[2];
+
+    const bool xi = x >= 1 && x < nx - 1, yi = y >= 1 && y < ny - 1, zi = z >= 1 && z < nz - 1;
+    const bool dx_on = x < nx - 1 && yi && zi;
+    const bool dy_on = xi && y < ny - 1 && zi;
+    bool dz_on = xi && yi && z < nz - 1;
+    const bool ex_on = x < nx - 1 && yi && zi;
+    const bool eyz_on = x >= 1 && z >= 1;
+
+    // soft source at this cell? (block-uniform screen first)
+    bool is_src = false;
+    if (c.nsources > 0) {
+        const int bx0 = blockIdx.x * TX, by0 = blockIdx.y * TY;
+        for (int s = 0; s < c.nsources; s++) {
+            const int sx_ = c.sources[3 * s], sy_ = c.sources[3 * s + 1], sz_ = c.sources[3 * s + 2];
+            if (sz_ == z && sx_ >= bx0 && sx_ < bx0 + TX && sy_ >= by0 && sy_ < by0 + TY)
+                is_src |= (sx_ == x && sy_ == y);
+        }
+    }
+    if (!ex_on && !eyz_on && !dx_on && !dy_on && !dz_on && !is_src)
+        return;
+
+    float dn[3], dp[3], dnew[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        dn[k] = c.d_cur[k][i];
+        dp[k] = c.d_prev[k][i];
+        dnew[k] = dp[k];  // untouched cells keep the slot's value
+    }
+    if (dx_on)
+        dnew[0] = dn[0] + c.ty * (hz[i] - hz[i - sy]) - c.tz * (hy[i] - hy[i - sz]);
+    if (dy_on)
+        dnew[1] = dn[1] + c.tz * (hx[i] - hx[i - sz]) - c.tx * (hz[i] - hz[i - sx]);
+    if (dz_on || is_src) {
+        dnew[2] = dn[2] + c.tx * (hy[i] - hy[i - sx]) - c.ty * (hx[i] - hx[i - sy]);
+        if (is_src) {
+            const int n = c.step_counter ? *c.step_counter : c.step;
+            const int j = source_sample_index(c, n);
+            dnew[2] = dnew[2] - ((j >= 0 && j < c.njz) ? c.jz[j] : 0.0f);
+        }
+        dz_on = true;
+    }
+    if (dx_on) c.d_prev[0][i] = dnew[0];
+    if (dy_on) c.d_prev[1][i] = dnew[1];
+    if (dz_on) c.d_prev[2][i] = dnew[2];
+
+    if (ex_on || eyz_on) {
+        const DebyeCoef k = load_coef(c.coef, c.mat[i]);
+#pragma unroll
+        for (int m = 0; m < 3; m++) {
+            if (m == 0 ? !ex_on : !eyz_on)
+                continue;
+            const float e0 = c.e_cur[m][i], e1 = c.e_prev[m][i];
+            c.e_prev[m][i] = debye_update(k, e0, e1, dnew[m], dn[m], dp[m]);
+        }
+    }
+}
+
+// updateMurBoundary over the face cells of the native state; the last block
+// to run cannot be known, so block (0, 0) advances the device step counter
+// (no other block of this launch reads it).
+__global__ void __launch_bounds__(256) native_mur_kernel(NativeConsts c)
+{
+    const int f = blockIdx.y;
+    const MurFace m = mur_face(f, c.nx, c.ny, c.nz);
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c.step_counter && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+        atomicAdd(c.step_counter, 1);
+    if (idx >= (long long)m.len_u * m.len_v)
+        return;
+    float *eT[3] = {c.e_prev[0], c.e_prev[1], c.e_prev[2]};
+    const float *eS[3] = {c.e_cur[0], c.e_cur[1], c.e_cur[2]};
+    mur_apply(f, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.dt, c.hx, c.hy, c.hz, c.me, c.rp, eT,
+              eS, c.scheme == FDTD_SCHEME_CORRECTED);
+}
+
+int launch_status()
+{
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FDTD_OK : (int)e;
+}
+
+bool fields_ok(const fdtd_native_fields *f, bool need_h_out)
+{
+    if (!f)
+        return false;
+    const float *const *ptrs = &f->hx;
+    for (int k = 0; k < 18; k++)
+        if (!ptrs[k] && (need_h_out || k < 3 || k >= 6))
+            return false;
+    return f->material != nullptr;
+}
+
+}  // namespace
+
+int launch_h(const NativeConsts &c, cudaStream_t s)
+{
+    const dim3 grid((c.nx + TX - 1) / TX, (c.ny + TY - 1) / TY, c.nz);
+    native_h_kernel<<<grid, dim3(TX, TY), 0, s>>>(c);
+    return launch_status();
+}
+
+int launch_de(const NativeConsts &c, cudaStream_t s)
+{
+    const dim3 grid((c.nx + TX - 1) / TX, (c.ny + TY - 1) / TY, c.nz);
+    native_de_kernel<<<grid, dim3(TX, TY), 0, s>>>(c);
+    return launch_status();
+}
+
+int launch_mur(const NativeConsts &c, cudaStream_t s)
+{
+    long long most = 0;
+    for (int f = 0; f < 12; f++) {
+        const MurFace m = mur_face(f, c.nx, c.ny, c.nz);
+        most = std::max(most, (long long)m.len_u * m.len_v);
+    }
+    native_mur_kernel<<<dim3((unsigned)((most + 255) / 256), 12), 256, 0, s>>>(c);
+    return launch_status();
+}
+
+}  // namespace fdtd
+
+using namespace fdtd;
+
+extern "C" {
+
+int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int scheme,
+                     const float *const rp_host[6], fdtd_plan **out)
+{
+    if (!p || !specs || !out || nclasses < 1 || nclasses > FDTD_MAX_CLASSES || p->nx < 3 || p->ny < 3 ||
+        p->nz < 3 || p->nz > 65535 || p->sourcesCount < 0 || p->sourcesCount > FDTD_MAX_SOURCES ||
+        (scheme != FDTD_SCHEME_REFERENCE && scheme != FDTD_SCHEME_CORRECTED))
+        return FDTD_ERR_INVALID;
+    for (int s = 0; s < p->sourcesCount; s++) {
+        const int *q = p->sources + 3 * s;
+        if (q[0] < 1 || q[0] >= p->nx || q[1] < 1 || q[1] >= p->ny || q[2] < 0 || q[2] >= p->nz)
+            return FDTD_ERR_INVALID;
+    }
+    fdtd_plan *plan = new (std::nothrow) fdtd_plan();
+    if (!plan)
+        return FDTD_ERR_NOMEM;
+    plan->nx = p->nx; plan->ny = p->ny; plan->nz = p->nz;
+    plan->dt = p->dt; plan->dx = p->dx; plan->dy = p->dy; plan->dz = p->dz;
+    plan->mu0 = p->mu0; plan->eps0 = p->eps0;
+    plan->scheme = scheme;
+    plan->nclasses = nclasses;
+    plan->nsources = p->sourcesCount;
+    for (int k = 0; k < 3 * p->sourcesCount; k++)
+        plan->sources[k] = p->sources[k];
+
+    // Debye coefficient table per class
+    std::vector<DebyeCoef> coef(nclasses);
+    for (int k = 0; k < nclasses; k++)
+        coef[k] = debye_coef(p->dt, p->eps0, specs[4 * k], specs[4 * k + 1], specs[4 * k + 2], specs[4 * k + 3], scheme);
+    plan->host_coef = coef;
+
+    // source table
+    std::vector<float> jz(FDTD_JZ_LEN, 0.0f);
+    if (p->jz && p->jzCount > 0) {
+        std::copy(p->jz, p->jz + std::min(p->jzCount, FDTD_JZ_LEN), jz.begin());
+    } else {
+        FdtdParams q = *p;
+        q.jz = nullptr;
+        q.jzCount = 0;
+        const int st = fdtd_setup_sources(&q);
+        if (st != FDTD_OK) {
+            delete plan;
+            return st;
+        }
+        std::copy(q.jz, q.jz + FDTD_JZ_LEN, jz.begin());
+        std::free(q.jz);
+    }
+    plan->njz = FDTD_JZ_LEN;
+
+    // Mur slabs (from the default material when not given, as the reference
+    // computes them before loadMaterials, fdtd.cu:59,65)
+    const size_t nrp[6] = {2 * (size_t)p->ny * p->nz, (size_t)p->nx * 2 * p->nz, (size_t)p->nx * p->ny * 2,
+                           2 * (size_t)p->ny * p->nz, (size_t)p->nx * 2 * p->nz, (size_t)p->nx * p->ny * 2};
+    std::vector<std::vector<float>> rp(6);
+    for (int k = 0; k < 6; k++)
+        rp[k].resize(nrp[k]);
+    if (rp_host) {
+        for (int k = 0; k < 6; k++) {
+            if (!rp_host[k]) {
+                delete plan;
+                return FDTD_ERR_INVALID;
+            }
+            std::copy(rp_host[k], rp_host[k] + nrp[k], rp[k].begin());
+        }
+    } else {
+        fdtd_setup_mur_uniform(p, p->defaultSigma, p->defaultEpsS, p->defaultEpsI, p->defaultTauD, rp[0].data(),
+                               rp[1].data(), rp[2].data(), rp[3].data(), rp[4].data(), rp[5].data());
+    }
+
+    size_t total = sizeof(DebyeCoef) * nclasses + sizeof(float) * FDTD_JZ_LEN;
+    size_t offs[8];
+    offs[0] = 0;
+    offs[1] = (sizeof(DebyeCoef) * nclasses + 255) & ~size_t(255);
+    size_t cur = offs[1] + ((sizeof(float) * FDTD_JZ_LEN + 255) & ~size_t(255));
+    for (int k = 0; k < 6; k++) {
+        offs[2 + k] = cur;
+        cur += (sizeof(float) * nrp[k] + 255) & ~size_t(255);
+    }
+    total = cur;
+    char *base = nullptr;
+    cudaError_t e = cudaMalloc(&base, total);
+    if (e != cudaSuccess) {
+        delete plan;
+        return e;
+    }
+    plan->d_block = base;
+    plan->d_coef = reinterpret_cast<DebyeCoef *>(base + offs[0]);
+    plan->d_jz = reinterpret_cast<float *>(base + offs[1]);
+    float *rpd[6];
+    for (int k = 0; k < 6; k++)
+        rpd[k] = reinterpret_cast<float *>(base + offs[2 + k]);
+    plan->rp = MurSlabs{rpd[0], rpd[1], rpd[2], rpd[3], rpd[4], rpd[5]};
+    e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * nclasses, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->d_jz, jz.data(), sizeof(float) * FDTD_JZ_LEN, cudaMemcpyHostToDevice);
+    for (int k = 0; k < 6 && e == cudaSuccess; k++)
+        e = cudaMemcpy(rpd[k], rp[k].data(), sizeof(float) * nrp[k], cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(base);
+        delete plan;
+        return e;
+    }
+    cudaGetDevice(&plan->device);
+    *out = plan;
+    return FDTD_OK;
+}
+
+int fdtd_plan_destroy(fdtd_plan *plan)
+{
+    if (!plan)
+        return FDTD_OK;
+    cudaError_t e = cudaFree(plan->d_block);
+    delete plan;
+    return e == cudaSuccess ? FDTD_OK : (int)e;
+}
+
+int fdtd_step_h(const fdtd_plan *plan, const fdtd_native_fields *f, fdtd_stream_t stream)
+{
+    if (!plan || !fields_ok(f, true))
+        return FDTD_ERR_INVALID;
+    return launch_h(make_consts(plan, f, 0), stream);
+}
+
+int fdtd_step_de(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd_stream_t stream)
+{
+    if (!plan || !fields_ok(f, true) || n < 0)
+        return FDTD_ERR_INVALID;
+    const NativeConsts c = make_consts(plan, f, n);
+    int st = launch_de(c, stream);
+    if (st == FDTD_OK)
+        st = launch_mur(c, stream);
+    return st;
+}
+
+int fdtd_step(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd_stream_t stream)
+{
+    if (!plan || !fields_ok(f, true) || n < 0)
+        return FDTD_ERR_INVALID;
+    for (int k = 0; k < 3; k++)
+        if ((&f->hx)[k] == (&f->hx_out)[k])
+            return FDTD_ERR_INVALID;
+    return launch_step(make_consts(plan, f, n), stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,68 @@
+// native.cuh -- plan object and kernel argument block of the native path.
+#pragma once
+
+#include <vector>
+
+#include "device_common.cuh"
+
+struct fdtd_plan {
+    int device = 0;
+    int nx = 0, ny = 0, nz = 0;
+    float dt = 0, dx = 0, dy = 0, dz = 0, mu0 = 0, eps0 = 0;
+    int scheme = FDTD_SCHEME_REFERENCE;
+    int nclasses = 0;
+    int nsources = 0;
+    int sources[3 * FDTD_MAX_SOURCES] = {};
+    int njz = 0;
+    std::vector<fdtd::DebyeCoef> host_coef;
+    char *d_block = nullptr;              // one allocation for everything below
+    fdtd::DebyeCoef *d_coef = nullptr;    // nclasses entries
+    float *d_jz = nullptr;                // FDTD_JZ_LEN entries
+    fdtd::MurSlabs rp{};                  // six Mur slabs
+};
+
+namespace fdtd {
+
+// Kernel argument block (passed by value).
+struct NativeConsts {
+    int nx, ny, nz;
+    float kx, ky, kz;      // dt / (mu0 d{x,y,z}) of the H update
+    float tx, ty, tz;      // dt / d{x,y,z} of the D update
+    float dt, hx, hy, hz;  // time step and cell sizes (Mur)
+    float me;              // mu0 * eps0 (Mur)
+    int scheme;
+    int nsources;
+    int sources[3 * FDTD_MAX_SOURCES];
+    const DebyeCoef *coef;
+    int nclasses;
+    const float *jz;
+    int njz;
+    MurSlabs rp;
+    int step;              // step index n when step_counter is null
+    int *step_counter;     // device step index (graph replay), may be null
+    const float *h_in[3];
+    float *h_out[3];
+    const float *e_cur[3];
+    float *e_prev[3];
+    const float *d_cur[3];
+    float *d_prev[3];
+    const uint8_t *mat;
+};
+
+NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n);
+
+int launch_h(const NativeConsts &c, cudaStream_t s);
+int launch_de(const NativeConsts &c, cudaStream_t s);
+int launch_mur(const NativeConsts &c, cudaStream_t s);
+// Single-pass step: H, D, sources and E in one z-marching kernel, then Mur.
+int launch_step(const NativeConsts &c, cudaStream_t s);
+
+// The kernels of one step in launch order, each launchable on its own (for
+// per-kernel event timing).
+struct StepKernel {
+    const char *name;
+    int (*launch)(const NativeConsts &, cudaStream_t);
+};
+int step_kernels(int kernel_kind, StepKernel *out, int max);
+
+}  // namespace fdtd

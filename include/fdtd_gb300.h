@@ -1,0 +1,327 @@
+/*
+ * fdtd_gb300.h -- C ABI of libfdtd_gb300.so, a GB300-native (sm_103a)
+ * implementation of the 3-D Yee FDTD time-step loop with single-pole Debye
+ * media and first-order Mur boundaries of rafalgrodzinski/fdtd.
+ *
+ * Conventions
+ *  - Every field is float32, structure of arrays, x fastest:
+ *    index = z*ny*nx + y*nx + x (the reference's OFFSET macro, utils.h:15).
+ *  - Device pointers are plain CUDA device addresses; streams are
+ *    cudaStream_t values (fdtd_stream_t, NULL = legacy default stream).
+ *  - Every entry point returns a status instead of exiting the process (the
+ *    reference's CHECK macro prints and calls exit, utils.h:5-13):
+ *    0 = success, 1..9999 = the cudaError_t of a failed CUDA call,
+ *    >= 10000 = an FDTD_ERR_* code below.
+ *  - Kernel launchers are asynchronous on the given stream; they return the
+ *    launch status (cudaGetLastError), not the completion status.
+ *  - Thread safety: functions that do not take an fdtd_solver may be called
+ *    from any host thread; one fdtd_solver must be driven from one thread.
+ */
+#ifndef FDTD_GB300_H
+#define FDTD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *fdtd_stream_t; /* identical to cudaStream_t */
+
+enum fdtd_status_code {
+    FDTD_OK = 0,
+    FDTD_ERR_INVALID = 10001,     /* argument or size out of range */
+    FDTD_ERR_IO = 10002,          /* a file could not be opened, read or written */
+    FDTD_ERR_FORMAT = 10003,      /* an input file does not follow the reference format */
+    FDTD_ERR_NO_SYMBOLS = 10004,  /* a compat launcher ran before fdtd_copy_symbols on this device */
+    FDTD_ERR_NOMEM = 10005,       /* a host allocation failed */
+    FDTD_ERR_STATE = 10006        /* call not valid in the object's current state */
+};
+
+/* Human-readable text for any status this library returns. */
+const char *fdtd_status_string(int status);
+
+/* Limits shared with the reference's constant block (fdtd_calculations.h:7-8). */
+#define FDTD_MAX_SOURCES 16
+#define FDTD_JZ_LEN 65536          /* host source table length (fdtd.cu:1031) */
+#define FDTD_MAX_CLASSES 256       /* material classes of the uint8 volume */
+
+/* Parameter block: same members, types and order as the reference's
+ * FdtdParams (fdtd.h:7-34), so a caller's struct can be passed unchanged. */
+typedef struct FdtdParams {
+    int nx, ny, nz;
+    int iterationsCount;
+    char *inputPath;
+    char *outputPath;
+    int elementsPerWave;
+    float waveFrequency;
+    float pulseWidth;
+    float pulseModulationFrequency;
+    int sourcesCount;
+    int *sources;                  /* 3*sourcesCount ints, 0-based x, y, z */
+    float defaultSigma;
+    float defaultEpsS;
+    float defaultEpsI;
+    float defaultTauD;
+    int jzCount;
+    float *jz;
+    float pi;
+    float c;
+    float timeskip;
+    float lambda;
+    float dt;
+    float dx, dy, dz;
+    float mu0;
+    float eps0;
+} FdtdParams;
+
+/* ------------------------------------------------------------------------
+ * Host set-up: the reference's input formats (all host memory).
+ * ---------------------------------------------------------------------- */
+
+/* Replaces initParamsWithPath (fdtd.cu:547-637): fixed line order, keys
+ * ignored, t_max rounded up to a multiple of 3, sources made 0-based, and
+ * c, dx = dy = dz, dt (timeskip 1.0), mu0, eps0 derived with the reference's
+ * float/double mix.  inputPath, outputPath and sources are malloc'd; release
+ * them with fdtd_params_free.  FDTD_ERR_FORMAT if a line does not scan. */
+int fdtd_params_read(const char *path, FdtdParams *out);
+
+/* Re-derives lambda, dx, dy, dz, dt, mu0 and eps0 with a time-step factor
+ * (the reference hard-codes timeskip = 1.0, fdtd.cu:627): dt is multiplied by
+ * timeskip exactly as the reference's formula does. */
+int fdtd_params_set_timeskip(FdtdParams *p, float timeskip);
+
+/* Frees the strings, the source list and the jz table of *p (replaces
+ * deallocParams, fdtd.cu:640-645) and zeroes those members. */
+void fdtd_params_free(FdtdParams *p);
+
+/* Replaces setupSources (fdtd.cu:1027-1082): allocates p->jz with
+ * FDTD_JZ_LEN floats and sets p->jzCount. */
+int fdtd_setup_sources(FdtdParams *p);
+
+/* Replaces setupMurBoundary (fdtd.cu:942-1024) over per-cell material arrays
+ * (nx*ny*nz each).  Slab shapes: rpx0/rpxEnd 2 x ny x nz, rpy0/rpyEnd
+ * nx x 2 x nz, rpz0/rpzEnd nx x ny x 2 (OFFSETRP, utils.h:16).  The reference
+ * calls it before loadMaterials (fdtd.cu:59,65), i.e. on the default
+ * material; pass default-filled arrays to reproduce that. */
+int fdtd_setup_mur(const FdtdParams *p, const float *sigma, const float *epsS, const float *epsI,
+                   const float *tauD, float *rpx0, float *rpy0, float *rpz0, float *rpxEnd,
+                   float *rpyEnd, float *rpzEnd);
+
+/* Same slabs for a volume made of one material (what the reference's call
+ * order produces): every entry gets the value of (sigma, epsS, epsI, tauD). */
+int fdtd_setup_mur_uniform(const FdtdParams *p, float sigma, float epsS, float epsI, float tauD,
+                           float *rpx0, float *rpy0, float *rpz0, float *rpxEnd, float *rpyEnd,
+                           float *rpzEnd);
+
+/* Reads a mat_specs file as loadMaterials does (fdtd.cu:878-904): at most 94
+ * records "code name sigma eps_s eps_i tau", a record that fails to scan
+ * repeats the previous one, reading stops after a code >= 94.  specs receives
+ * FDTD_MAX_CLASSES x 4 floats (sigma, eps_s, eps_i, tau; unlisted codes 0). */
+int fdtd_read_specs(const char *specsPath, float *specs);
+
+/* Replaces the voxel half of loadMaterials (fdtd.cu:909-936) in the native
+ * form: nz slices <materialsPath>/v1_%05d.pgm (1-based), each a 6-token
+ * header then nx*ny codes read as one flat stream (the header's width and
+ * height are not used).  codes receives nx*ny*nz uint8 class indices.
+ * Slices are parsed in parallel with nthreads host threads (0 = all cores).
+ * FDTD_ERR_FORMAT on a short slice or a code outside 0..255. */
+int fdtd_load_material_codes(const FdtdParams *p, const char *materialsPath, uint8_t *codes,
+                             int nthreads);
+
+/* Replaces loadMaterials (fdtd.cu:875-939) in the reference's form: four
+ * per-cell float arrays looked up from the specs table. */
+int fdtd_load_materials(const FdtdParams *p, const char *specsPath, const char *materialsPath,
+                        float *sigma, float *epsS, float *epsI, float *tauD);
+
+/* Replaces writeResults3d (fdtd.cu:1288-1494): for H, D, E and x, y, z one
+ * text file per z plane, <outputPath>/{H|D|E}_field_{x|y|z}_%05d_z%05d.out
+ * (0-based iteration, plane), ny lines of nx values " % 9.3E".  Any field
+ * pointer may be NULL to skip it.  Files are formatted by nthreads host
+ * threads (0 = all cores); the bytes are identical to the reference's. */
+int fdtd_write_results3d(const FdtdParams *p, const float *hx, const float *hy, const float *hz,
+                         const float *dx, const float *dy, const float *dz, const float *ex,
+                         const float *ey, const float *ez, int iteration, int nthreads);
+
+/* ------------------------------------------------------------------------
+ * Reference-compatible kernel launchers (fdtd_calculations.h:18-42).
+ * Same argument lists, roles and per-component index ranges as the
+ * reference kernels; each reads the parameter block that fdtd_copy_symbols
+ * stored for the current device.  Target and source buffers must not alias
+ * (except as the reference itself passes them).
+ * ---------------------------------------------------------------------- */
+
+/* Replaces copySymbolsToDevice (fdtd_calculations.cu:7-29): grid size, dt,
+ * dx, dy, dz, mu0, eps0, sources (FDTD_ERR_INVALID beyond FDTD_MAX_SOURCES,
+ * where the reference would read past dSources) and the whole jz table (the
+ * reference keeps jz[0..511] only, so its iterations >= 512 are undefined). */
+int fdtd_copy_symbols(const FdtdParams *p);
+
+/* updateHField (fdtd_calculations.cu:32-77): H -= dt/mu0 curl E^n, in place. */
+int fdtd_update_h(float *hx, float *hy, float *hz, const float *exSource, const float *eySource,
+                  const float *ezSource, fdtd_stream_t stream);
+
+/* updateDField (fdtd_calculations.cu:80-122): D_target = D_source + dt curl H. */
+int fdtd_update_d(float *dxTarget, float *dyTarget, float *dzTarget, const float *dxSource,
+                  const float *dySource, const float *dzSource, const float *hx, const float *hy,
+                  const float *hz, fdtd_stream_t stream);
+
+/* updateEField (fdtd_calculations.cu:125-184): Debye E update from E^n
+ * (Source0), E^{n-1} (Source1), D^{n+1} (dSource0), D^n, D^{n-1} and the
+ * per-cell sigma, eps_inf, eps_s, tau. */
+int fdtd_update_e(float *exTarget, float *eyTarget, float *ezTarget, const float *exSource0,
+                  const float *eySource0, const float *ezSource0, const float *exSource1,
+                  const float *eySource1, const float *ezSource1, const float *dxSource0,
+                  const float *dySource0, const float *dzSource0, const float *dxSource1,
+                  const float *dySource1, const float *dzSource1, const float *dxSource2,
+                  const float *dySource2, const float *dzSource2, const float *sigma,
+                  const float *epsI, const float *epsS, const float *tauD, fdtd_stream_t stream);
+
+/* updateSources (fdtd_calculations.cu:187-213): Dz at each source cell =
+ * Dz_source + curl - jz[currIteration].  One warp, not a full-grid launch. */
+int fdtd_update_sources(float *dzTarget, const float *dzSource, const float *hx, const float *hy,
+                        int currIteration, fdtd_stream_t stream);
+
+/* updateMurBoundary (fdtd_calculations.cu:216-428): first-order Mur on the
+ * tangential E of the six faces, edges excluded, including the reference's
+ * ey x = nx-1 term that reads eySource at x-1 twice (:323).  Launched over
+ * the face cells only. */
+int fdtd_update_mur(float *exTarget, float *eyTarget, float *ezTarget, const float *exSource,
+                    const float *eySource, const float *ezSource, const float *rpx0,
+                    const float *rpy0, const float *rpz0, const float *rpxEnd, const float *rpyEnd,
+                    const float *rpzEnd, fdtd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Native fused path: uint8 material classes, two E and two D slots updated
+ * in place, fused kernels.  No reference counterpart; it computes the same
+ * step as the five kernels above (same ranges, same order of effects).
+ * ---------------------------------------------------------------------- */
+
+/* Scheme: FDTD_SCHEME_REFERENCE reproduces the reference exactly, including
+ * its E^n coefficient d = 2b - sigma dt^2 (|E| doubles every step in vacuum),
+ * the ey Mur term at x = nx-1 and the source sample jz[n - n%3].
+ * FDTD_SCHEME_CORRECTED uses d = a + b - sigma dt^2, the E^{n+1} term on
+ * that Mur face and jz[n]. */
+enum { FDTD_SCHEME_REFERENCE = 0, FDTD_SCHEME_CORRECTED = 1 };
+
+/* Per-run constants on the device: Debye coefficients per material class,
+ * sources, the jz table and the Mur slabs.  Created once, read by the native
+ * kernels; immutable afterwards. */
+typedef struct fdtd_plan fdtd_plan;
+
+/* specs: nclasses x 4 floats (sigma, eps_s, eps_i, tau).  rp: the six Mur
+ * slabs on the host (NULL: computed from p's default material, as the
+ * reference does).  jz: p->jz if non-NULL, else built by fdtd_setup_sources. */
+int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int scheme,
+                     const float *const rp_host[6], fdtd_plan **out);
+int fdtd_plan_destroy(fdtd_plan *plan);
+
+/* Device state of the native path.  E and D keep two slots each: the
+ * "prev" slot holds step n-1 on entry and receives step n+1. */
+typedef struct fdtd_native_fields {
+    float *hx, *hy, *hz;                /* H^{n-1/2} on entry */
+    float *hx_out, *hy_out, *hz_out;    /* receives H^{n+1/2} */
+    float *ex, *ey, *ez;                /* E^n, read only */
+    float *ex_prev, *ey_prev, *ez_prev; /* E^{n-1} in, E^{n+1} out */
+    float *dx, *dy, *dz;                /* D^n, read only */
+    float *dx_prev, *dy_prev, *dz_prev; /* D^{n-1} in, D^{n+1} out */
+    const uint8_t *material;            /* class per cell */
+} fdtd_native_fields;
+
+/* H half step (fused three components).  hx_out may equal hx (in place). */
+int fdtd_step_h(const fdtd_plan *plan, const fdtd_native_fields *f, fdtd_stream_t stream);
+
+/* D update, sources (sample for step index n), Debye E update and the Mur
+ * faces of step n.  Reads H^{n+1/2} from hx_out..hz_out. */
+int fdtd_step_de(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd_stream_t stream);
+
+/* Whole step n in one z-marching pass plus the Mur faces.  hx_out..hz_out
+ * must not alias hx..hz (H is double-buffered). */
+int fdtd_step(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd_stream_t stream);
+
+/* ------------------------------------------------------------------------
+ * Solver handle: owns the device state of one solve, runs the step loop as
+ * a CUDA graph and streams snapshots through pinned buffers on a side stream.
+ * ---------------------------------------------------------------------- */
+
+typedef struct fdtd_solver fdtd_solver;
+
+enum {
+    FDTD_KERNEL_SINGLE_PASS = 0,  /* fdtd_step: one z-marching kernel per step */
+    FDTD_KERNEL_TWO_PASS = 1      /* fdtd_step_h + fdtd_step_de */
+};
+
+/* Field selectors; bit (1 << FDTD_FIELD_x) in snapshot masks. */
+enum {
+    FDTD_FIELD_HX = 0, FDTD_FIELD_HY, FDTD_FIELD_HZ,
+    FDTD_FIELD_DX, FDTD_FIELD_DY, FDTD_FIELD_DZ,
+    FDTD_FIELD_EX, FDTD_FIELD_EY, FDTD_FIELD_EZ,
+    FDTD_FIELD_COUNT
+};
+
+typedef struct fdtd_solver_config {
+    const FdtdParams *params;   /* grid, constants, sources, optional jz */
+    const uint8_t *material;    /* host: nx*ny*nz class indices */
+    const float *specs;         /* host: nclasses x 4 (sigma, eps_s, eps_i, tau) */
+    int nclasses;
+    int scheme;                 /* FDTD_SCHEME_* */
+    int kernel;                 /* FDTD_KERNEL_* */
+    int device;                 /* CUDA device ordinal */
+} fdtd_solver_config;
+
+int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out);
+int fdtd_solver_destroy(fdtd_solver *s);
+
+/* Enqueue nsteps steps on the solver's stream (asynchronous). */
+int fdtd_solver_run(fdtd_solver *s, int nsteps);
+int fdtd_solver_synchronize(fdtd_solver *s);
+
+/* Number of completed-or-enqueued steps. */
+int fdtd_solver_steps(const fdtd_solver *s);
+
+/* Copies the current value of one field (after the last enqueued step) into
+ * host memory (nx*ny*nz floats); synchronises the solver first. */
+int fdtd_solver_get_field(fdtd_solver *s, int field, float *host_out);
+
+/* The solver's CUDA stream (cudaStream_t). */
+fdtd_stream_t fdtd_solver_stream(const fdtd_solver *s);
+
+/* Snapshot callback: called on a library thread with the step index (0-based,
+ * the step just completed), the field id and nx*ny*nplanes floats in pinned
+ * host memory that stay valid until the callback returns. */
+typedef void (*fdtd_snapshot_fn)(void *user, int step, int field, const float *data, int z0, int nplanes);
+
+typedef struct fdtd_snapshot_spec {
+    int every;                  /* 0 disables; else every `every` steps */
+    uint32_t field_mask;        /* bits 1 << FDTD_FIELD_* */
+    int z0, nplanes;            /* z range copied; nplanes 0 = whole volume */
+    fdtd_snapshot_fn callback;  /* NULL: write the reference text layout */
+    void *user;
+    const char *output_dir;     /* used when callback is NULL */
+    int writer_threads;         /* text formatting threads (0 = all cores) */
+} fdtd_snapshot_spec;
+
+/* Installs (or with every == 0 removes) the snapshot schedule.  Device-to-host
+ * copies run on a side stream into a pinned ring and overlap the next step. */
+int fdtd_solver_set_snapshots(fdtd_solver *s, const fdtd_snapshot_spec *spec);
+
+/* Waits for every snapshot of enqueued steps to be delivered. */
+int fdtd_solver_flush_snapshots(fdtd_solver *s);
+
+/* Kernel timing (the role of the reference's nvprof job scripts,
+ * run_fdtd_prof*-rafal.sh): runs nsteps steps launching each kernel directly,
+ * bracketed by CUDA events on the solver stream, and returns the average
+ * duration in milliseconds of each of the step's kernels in launch order
+ * (at most max_kernels; *nkernels receives the count).  The steps advance
+ * the solve like fdtd_solver_run. */
+int fdtd_solver_profile(fdtd_solver *s, int nsteps, float *avg_ms, int max_kernels, int *nkernels);
+
+/* Name of kernel k of a step, as reported by fdtd_solver_profile. */
+const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FDTD_GB300_H */

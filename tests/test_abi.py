@@ -1,0 +1,46 @@
+"""The C-ABI library loads and exports every entry point its header declares."""
+from __future__ import annotations
+
+import re
+import subprocess
+from pathlib import Path
+
+import fdtd_gb300 as fg
+
+HEADER_DIR = Path(__file__).resolve().parent.parent / "include"
+
+
+def declared_functions() -> set[str]:
+    names = set()
+    for h in HEADER_DIR.glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        text = re.sub(r"typedef[^;]*;", "", text)
+        names |= set(re.findall(r"\b(fdtd_[a-z0-9_]+)\s*\(", text))
+    return names
+
+
+def test_library_exports_every_declared_function():
+    names = declared_functions()
+    assert len(names) >= 30
+    L = fg.lib()
+    missing = [n for n in sorted(names) if not hasattr(L, n)]
+    assert not missing, missing
+    out = subprocess.run(["nm", "-D", "--defined-only", str(fg.LIB_PATH)], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (fdtd_[a-z0-9_]+)\b", out))
+    assert names <= exported, sorted(names - exported)
+
+
+def test_status_strings():
+    L = fg.lib()
+    assert L.fdtd_status_string(0) == b"success"
+    assert b"format" in L.fdtd_status_string(fg.FDTD_ERR_FORMAT)
+    assert L.fdtd_status_string(2)  # a CUDA error code
+
+
+def test_invalid_arguments_return_status_without_a_gpu():
+    L = fg.lib()
+    assert L.fdtd_params_read(None, None) == fg.FDTD_ERR_INVALID
+    assert L.fdtd_setup_sources(None) == fg.FDTD_ERR_INVALID
+    assert L.fdtd_plan_create(None, None, 0, 0, None, None) == fg.FDTD_ERR_INVALID
+    assert L.fdtd_solver_create(None, None) == fg.FDTD_ERR_INVALID
+    assert L.fdtd_step(None, None, 0, None) == fg.FDTD_ERR_INVALID

@@ -1,0 +1,69 @@
+"""Native fused path (fdtd_step, fdtd_step_h + fdtd_step_de) through the C ABI
+against the reference's golden runs and the oracle."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import fdtd_gb300 as fg
+from oracle import pyoracle as po
+
+from .gpu_util import make_params, run_native
+from .helpers import REL_L2_TOL, assert_fields_close, class_media, load_run, random_case
+
+pytestmark = pytest.mark.gpu
+
+CLASS_RUNS = ["sphere24", "classes70x20x9"]
+
+
+@pytest.mark.parametrize("mode", ["single", "two_pass"])
+@pytest.mark.parametrize("name", CLASS_RUNS)
+def test_native_matches_reference_run(cuda, name, mode):
+    g = load_run(name)
+    raw = make_params(g.dims, g.consts, g.sources, g.jz)
+    got = run_native(cuda, raw, g.specs, g.codes, g.media.rp, g.steps, mode=mode)
+    assert_fields_close(got, g.latest())
+
+
+@pytest.mark.parametrize("mode", ["single", "two_pass"])
+@pytest.mark.parametrize("dims,seed", [((33, 17, 12), 1), ((64, 9, 7), 2), ((5, 40, 6), 3), ((129, 3, 4), 4)])
+def test_native_matches_fp32_oracle_reference_scheme(cuda, dims, seed, mode):
+    nx, ny, nz = dims
+    codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, seed, nsrc=3)
+    steps = 14
+    media = class_media(codes, specs, rp)
+    st = po.State(nx, ny, nz, np.float32)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts), media, st, 0, steps)
+    want = st.latest(steps)
+    raw = make_params(dims, consts, sources, jz)
+    got = run_native(cuda, raw, specs, codes, rp, steps, mode=mode)
+    assert_fields_close(got, want)
+
+
+@pytest.mark.parametrize("mode", ["single", "two_pass"])
+def test_native_corrected_scheme_matches_fp64_oracle(cuda, mode):
+    dims = (41, 23, 19)
+    nx, ny, nz = dims
+    codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, 7, nsrc=2)
+    steps = 60
+    media = class_media(codes, specs, rp)
+    st = po.State(nx, ny, nz, np.float64)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts, corrected=True), media, st, 0, steps)
+    want = st.latest(steps)
+    raw = make_params(dims, consts, sources, jz)
+    got = run_native(cuda, raw, specs, codes, rp, steps, scheme=fg.SCHEME_CORRECTED, mode=mode)
+    assert_fields_close(got, want, tol=REL_L2_TOL)
+
+
+def test_single_pass_rejects_in_place_h(cuda):
+    import ctypes as C
+
+    from .gpu_util import NativeState, Params
+
+    g = load_run("sphere24")
+    raw = make_params(g.dims, g.consts, g.sources, g.jz)
+    plan = fg.Plan(Params(raw), g.specs, rp=g.media.rp)
+    st = NativeState(cuda, Params(raw).shape, g.codes)
+    f = st.fields(0, single_pass=False)  # H in place
+    assert fg.lib().fdtd_step(plan.handle, C.byref(f), 0, None) == fg.FDTD_ERR_INVALID
+    plan.close()

@@ -1,0 +1,117 @@
+"""Solver handle (graph-replayed step loop, snapshots) against the golden runs
+and the FP64 oracle, driven from the reference's input files."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import fdtd_gb300 as fg
+from fdtd_gb300 import phantom as ph
+from oracle import pyoracle as po
+
+from .helpers import REL_L2_TOL, assert_fields_close, load_run, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+KERNELS = [fg.KERNEL_SINGLE_PASS, fg.KERNEL_TWO_PASS]
+
+
+def solver_from_files(root, n, t_max, kernel, scheme=fg.SCHEME_REFERENCE, timeskip=None):
+    path = ph.c1_inputs(root, n=n, t_max=t_max)
+    p = fg.Params.read(path)
+    if timeskip is not None:
+        p.set_timeskip(timeskip)
+    codes = fg.load_material_codes(p, root / "pgm")
+    specs = fg.read_specs(root / "mat_specs")
+    return p, codes, specs, fg.Solver(p, codes, specs, scheme=scheme, kernel=kernel, nclasses=2)
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_solver_from_reference_files_matches_reference_run(cuda, tmp_path, kernel):
+    g = load_run("sphere24")
+    p, codes, specs, s = solver_from_files(tmp_path, 24, 60, kernel)
+    assert np.array_equal(codes, g.codes)
+    for chunk in (5, 17, 26):  # uneven chunks exercise both graph parities
+        s.run(chunk)
+    assert s.steps == g.steps == 48
+    assert_fields_close(s.fields(), g.latest())
+    s.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_snapshots_equal_field_reads(cuda, tmp_path, kernel):
+    p, codes, specs, a = solver_from_files(tmp_path / "a", 20, 30, kernel)
+    got = {}
+    a.set_snapshots(every=5, fields=("ex", "hz", "dz"), z0=3, nplanes=4,
+                    callback=lambda step, name, data: got.__setitem__((step, name), data))
+    a.run(23)
+    a.flush_snapshots()
+    assert sorted({k[0] for k in got}) == [0, 5, 10, 15, 20]
+    _, _, _, b = solver_from_files(tmp_path / "b", 20, 30, kernel)
+    done = 0
+    for step in (0, 5, 10, 15, 20):
+        b.run(step + 1 - done)
+        done = step + 1
+        for name in ("ex", "hz", "dz"):
+            assert np.array_equal(got[(step, name)], b.field(name)[3:7]), (step, name)
+    a.close()
+    b.close()
+
+
+def test_text_snapshots_in_reference_layout(cuda, tmp_path):
+    p, codes, specs, s = solver_from_files(tmp_path, 12, 9, fg.KERNEL_SINGLE_PASS)
+    out = tmp_path / "out"
+    out.mkdir()
+    s.set_snapshots(every=1, fields=fg.FIELDS, output_dir=out)
+    s.run(3)
+    s.flush_snapshots()
+    names = sorted(q.name for q in out.iterdir())
+    assert len(names) == 3 * 9 * 12
+    assert names[0] == "D_field_x_00000_z00000.out"
+    ez = s.field("ez")
+    text = (out / "E_field_z_00002_z00006.out").read_text()
+    want = "".join("".join(" % 9.3E" % float(v) for v in row) + "\n" for row in ez[6])
+    assert text == want
+    s.close()
+
+
+def test_c1_sphere_corrected_scheme_500_steps_vs_fp64_oracle(cuda, tmp_path):
+    """64^3 sphere, dt = 0.99 of the Courant limit, corrected Debye scheme,
+    501 steps: relative L2 of every field against the FP64 oracle."""
+    p, codes, specs, s = solver_from_files(tmp_path, 64, 500, fg.KERNEL_SINGLE_PASS, scheme=fg.SCHEME_CORRECTED,
+                                           timeskip=0.99)
+    steps = p.iterationsCount
+    assert steps == 501
+    s.run(steps)
+    got = s.fields()
+    s.close()
+    q = po.params_read(tmp_path / "input_params", "f64")
+    q.dt = p.dt
+    jz = p.setup_sources()
+    media = po.Media(*(np.ascontiguousarray(specs[codes, k]) for k in (0, 2, 1, 3)))
+    media.rp = po.uniform_media(q).rp
+    cfg = po.make_cfg(q, jz, corrected=True)
+    st = po.State(64, 64, 64, np.float64)
+    po.run(cfg, media, st, 0, steps)
+    want = st.latest(steps)
+    assert all(np.all(np.isfinite(v)) for v in want.values())
+    assert max(np.abs(v).max() for v in want.values()) > 0
+    assert_fields_close(got, want, tol=REL_L2_TOL)
+
+
+def test_c1_sphere_reference_scheme_finite_window(cuda, tmp_path):
+    """Reference scheme on the 64^3 sphere: identical to the FP32 oracle
+    (which reproduces the reference kernels) while the fields are finite."""
+    p, codes, specs, s = solver_from_files(tmp_path, 64, 60, fg.KERNEL_SINGLE_PASS)
+    s.run(60)
+    got = s.fields()
+    s.close()
+    q = po.params_read(tmp_path / "input_params", "f32")
+    jz = p.setup_sources()
+    media = po.Media(*(np.ascontiguousarray(specs[codes, k]) for k in (0, 2, 1, 3)))
+    media.rp = po.uniform_media(q).rp
+    st = po.State(64, 64, 64, np.float32)
+    po.run(po.make_cfg(q, jz), media, st, 0, 60)
+    want = st.latest(60)
+    assert all(np.all(np.isfinite(v)) for v in want.values())
+    assert_fields_close(got, want)
