@@ -282,8 +282,9 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
     for (int k = 0; k < 3 * p->sourcesCount; k++)
         plan->sources[k] = p->sources[k];
 
-    // Debye coefficient table per class
-    std::vector<DebyeCoef> coef(nclasses);
+    // Debye coefficient table per class; all 256 entries exist so that any
+    // uint8 class index reads inside the table (unused entries are zero)
+    std::vector<DebyeCoef> coef(FDTD_MAX_CLASSES, DebyeCoef{});
     for (int k = 0; k < nclasses; k++)
         coef[k] = debye_coef(p->dt, p->eps0, specs[4 * k], specs[4 * k + 1], specs[4 * k + 2], specs[4 * k + 3], scheme);
     plan->host_coef = coef;
@@ -326,10 +327,10 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
                                rp[1].data(), rp[2].data(), rp[3].data(), rp[4].data(), rp[5].data());
     }
 
-    size_t total = sizeof(DebyeCoef) * nclasses + sizeof(float) * FDTD_JZ_LEN;
+    size_t total = 0;
     size_t offs[8];
     offs[0] = 0;
-    offs[1] = (sizeof(DebyeCoef) * nclasses + 255) & ~size_t(255);
+    offs[1] = (sizeof(DebyeCoef) * FDTD_MAX_CLASSES + 255) & ~size_t(255);
     size_t cur = offs[1] + ((sizeof(float) * FDTD_JZ_LEN + 255) & ~size_t(255));
     for (int k = 0; k < 6; k++) {
         offs[2 + k] = cur;
@@ -349,7 +350,7 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
     for (int k = 0; k < 6; k++)
         rpd[k] = reinterpret_cast<float *>(base + offs[2 + k]);
     plan->rp = MurSlabs{rpd[0], rpd[1], rpd[2], rpd[3], rpd[4], rpd[5]};
-    e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * nclasses, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(plan->d_jz, jz.data(), sizeof(float) * FDTD_JZ_LEN, cudaMemcpyHostToDevice);
     for (int k = 0; k < 6 && e == cudaSuccess; k++)

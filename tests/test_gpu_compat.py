@@ -69,7 +69,8 @@ def test_each_compat_kernel_matches_oracle(cuda):
     h = [rnd() for _ in range(3)]
     e = [rnd() for _ in range(3)]
     hd = [dev(torch, a) for a in h]
-    fg.check(L.fdtd_update_h(*[ptr(t) for t in hd], *[ptr(dev(torch, a)) for a in e], None))
+    ed = [dev(torch, a) for a in e]  # keep every device buffer referenced until the launch completes
+    fg.check(L.fdtd_update_h(*[ptr(t) for t in hd], *[ptr(t) for t in ed], None))
     lib32.oracle_update_h(C.byref(cfg), arr3(h), arr3(e))
     torch.cuda.synchronize()
     for a, b in zip(hd, h):
@@ -80,8 +81,9 @@ def test_each_compat_kernel_matches_oracle(cuda):
     dS = [rnd() for _ in range(3)]
     dTd = [zeros(torch, sh) for _ in range(3)]
     hdv = [dev(torch, a) for a in h]
-    fg.check(L.fdtd_update_d(*[ptr(t) for t in dTd], *[ptr(dev(torch, a)) for a in dS], *[ptr(t) for t in hdv], None))
-    fg.check(L.fdtd_update_sources(ptr(dTd[2]), ptr(dev(torch, dS[2])), ptr(hdv[0]), ptr(hdv[1]), 6, None))
+    dSd = [dev(torch, a) for a in dS]
+    fg.check(L.fdtd_update_d(*[ptr(t) for t in dTd], *[ptr(t) for t in dSd], *[ptr(t) for t in hdv], None))
+    fg.check(L.fdtd_update_sources(ptr(dTd[2]), ptr(dSd[2]), ptr(hdv[0]), ptr(hdv[1]), 6, None))
     lib32.oracle_update_d(C.byref(cfg), arr3(dT), arr3(dS), arr3(h), 6)
     torch.cuda.synchronize()
     for a, b in zip(dTd, dT):
@@ -92,8 +94,8 @@ def test_each_compat_kernel_matches_oracle(cuda):
     srcs = [[rnd() for _ in range(3)] for _ in range(5)]
     eTd = [zeros(torch, sh) for _ in range(3)]
     md = [dev(torch, a) for a in (media.sigma, media.eps_i, media.eps_s, media.tau_d)]
-    fg.check(L.fdtd_update_e(*[ptr(t) for t in eTd], *[ptr(dev(torch, a)) for s in srcs for a in s],
-                             *[ptr(t) for t in md], None))
+    srcd = [dev(torch, a) for s in srcs for a in s]
+    fg.check(L.fdtd_update_e(*[ptr(t) for t in eTd], *[ptr(t) for t in srcd], *[ptr(t) for t in md], None))
     ms = media.as_struct()
     lib32.oracle_update_e(C.byref(cfg), C.byref(ms), arr3(eT), *[arr3(s) for s in srcs])
     torch.cuda.synchronize()
@@ -105,7 +107,8 @@ def test_each_compat_kernel_matches_oracle(cuda):
     eT2 = [rnd() for _ in range(3)]
     eT2d = [dev(torch, a) for a in eT2]
     rpd = [dev(torch, r) for r in rp]
-    fg.check(L.fdtd_update_mur(*[ptr(t) for t in eT2d], *[ptr(dev(torch, a)) for a in eS], *[ptr(t) for t in rpd], None))
+    eSd = [dev(torch, a) for a in eS]
+    fg.check(L.fdtd_update_mur(*[ptr(t) for t in eT2d], *[ptr(t) for t in eSd], *[ptr(t) for t in rpd], None))
     lib32.oracle_update_mur(C.byref(cfg), C.byref(ms), arr3(eT2), arr3(eS))
     torch.cuda.synchronize()
     for a, b in zip(eT2d, eT2):
