@@ -33,6 +33,7 @@ FDTD_ERR_FORMAT = 10003
 FDTD_ERR_NO_SYMBOLS = 10004
 FDTD_ERR_NOMEM = 10005
 FDTD_ERR_STATE = 10006
+FDTD_ERR_DEVICE_TIMEOUT = 10007
 MAX_SOURCES = 16
 JZ_LEN = 65536
 MAX_CLASSES = 256
@@ -129,6 +130,7 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_update_mur", _I, *([_V] * 12), _V)
         _sig(L, "fdtd_plan_create", _I, PP, _P, _I, _I, C.POINTER(_P), C.POINTER(_V))
         _sig(L, "fdtd_plan_destroy", _I, _V)
+        _sig(L, "fdtd_plan_status", _I, _V)
         _sig(L, "fdtd_step_h", _I, _V, C.POINTER(NativeFields), _V)
         _sig(L, "fdtd_step_de", _I, _V, C.POINTER(NativeFields), _I, _V)
         _sig(L, "fdtd_step", _I, _V, C.POINTER(NativeFields), _I, _V)

@@ -65,6 +65,7 @@ NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)
     c.rp = p->rp;
     c.step = n;
     c.step_counter = nullptr;
+    c.err = p->d_err;
     if (f) {
         for (int k = 0; k < 3; k++) {
             c.h_in[k] = (&f->hx)[k];
@@ -252,6 +253,19 @@ int launch_mur(const NativeConsts &c, cudaStream_t s)
     return launch_status();
 }
 
+int plan_error(const fdtd_plan *p)
+{
+    int flag = 0;
+    cudaError_t e = cudaMemcpy(&flag, p->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return e;
+    if (flag) {
+        cudaMemset(p->d_err, 0, sizeof(int));
+        return FDTD_ERR_DEVICE_TIMEOUT;
+    }
+    return FDTD_OK;
+}
+
 }  // namespace fdtd
 
 using namespace fdtd;
@@ -336,7 +350,8 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
         offs[2 + k] = cur;
         cur += (sizeof(float) * nrp[k] + 255) & ~size_t(255);
     }
-    total = cur;
+    const size_t err_off = cur;
+    total = cur + 256;
     char *base = nullptr;
     cudaError_t e = cudaMalloc(&base, total);
     if (e != cudaSuccess) {
@@ -350,7 +365,10 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
     for (int k = 0; k < 6; k++)
         rpd[k] = reinterpret_cast<float *>(base + offs[2 + k]);
     plan->rp = MurSlabs{rpd[0], rpd[1], rpd[2], rpd[3], rpd[4], rpd[5]};
-    e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES, cudaMemcpyHostToDevice);
+    plan->d_err = reinterpret_cast<int *>(base + err_off);
+    e = cudaMemset(plan->d_err, 0, sizeof(int));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(plan->d_jz, jz.data(), sizeof(float) * FDTD_JZ_LEN, cudaMemcpyHostToDevice);
     for (int k = 0; k < 6 && e == cudaSuccess; k++)
@@ -363,6 +381,16 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
     cudaGetDevice(&plan->device);
     *out = plan;
     return FDTD_OK;
+}
+
+int fdtd_plan_status(fdtd_plan *plan)
+{
+    if (!plan)
+        return FDTD_ERR_INVALID;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess)
+        return e;
+    return plan_error(plan);
 }
 
 int fdtd_plan_destroy(fdtd_plan *plan)

@@ -19,6 +19,7 @@ struct fdtd_plan {
     fdtd::DebyeCoef *d_coef = nullptr;    // nclasses entries
     float *d_jz = nullptr;                // FDTD_JZ_LEN entries
     fdtd::MurSlabs rp{};                  // six Mur slabs
+    int *d_err = nullptr;                 // device error flag
 };
 
 namespace fdtd {
@@ -40,6 +41,7 @@ struct NativeConsts {
     MurSlabs rp;
     int step;              // step index n when step_counter is null
     int *step_counter;     // device step index (graph replay), may be null
+    int *err;              // device error flag (a bounded wait gave up)
     const float *h_in[3];
     float *h_out[3];
     const float *e_cur[3];
@@ -64,5 +66,8 @@ struct StepKernel {
     int (*launch)(const NativeConsts &, cudaStream_t);
 };
 int step_kernels(int kernel_kind, StepKernel *out, int max);
+
+// Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
+int plan_error(const fdtd_plan *p);
 
 }  // namespace fdtd

@@ -435,7 +435,10 @@ int fdtd_solver_synchronize(fdtd_solver *s)
     if (!s)
         return FDTD_ERR_INVALID;
     cudaSetDevice(s->device);
-    return cu(cudaStreamSynchronize(s->stream));
+    int st = cu(cudaStreamSynchronize(s->stream));
+    if (st == FDTD_OK)
+        st = plan_error(s->plan);
+    return st;
 }
 
 int fdtd_solver_steps(const fdtd_solver *s) { return s ? s->steps : -1; }
@@ -446,9 +449,7 @@ int fdtd_solver_get_field(fdtd_solver *s, int field, float *host_out)
 {
     if (!s || !host_out || field < 0 || field >= FDTD_FIELD_COUNT)
         return FDTD_ERR_INVALID;
-    int st = cu(cudaSetDevice(s->device));
-    if (st == FDTD_OK)
-        st = cu(cudaStreamSynchronize(s->stream));
+    int st = fdtd_solver_synchronize(s);
     if (st == FDTD_OK)
         st = cu(cudaMemcpy(host_out, field_buffer(s, field, s->steps), sizeof(float) * s->ncell,
                            cudaMemcpyDeviceToHost));

@@ -1,15 +1,528 @@
-// step_fused.cu -- single-pass step (H, D, sources, E) followed by Mur.
+// step_fused.cu -- the single-pass step: H, D, sources and the Debye E update
+// of one Yee step in one z-marching kernel, followed by the Mur face kernel.
+//
+// Each CTA owns a 32 x TY column tile of (x, y) and a chunk of z planes.  Per
+// plane it stages, in shared memory, E^n with a one-cell halo on every side,
+// H^{n-1/2} with a one-cell halo at low x and low y, and the tile's D^n,
+// D^{n-1}, E^{n-1} and material classes.  It recomputes H^{n+1/2} on its low
+// halo, so that D^{n+1} = D^n + dt curl H^{n+1/2} needs no neighbour tile's
+// output; H is double-buffered (read H_old, write H_new), E and D are updated
+// in their "prev" slots.  Every array is therefore read once and written once
+// per step: 15 floats + 1 byte read, 9 floats written, 97 bytes per cell.
+//
+// Staging: with nx a multiple of 16 and 16-byte aligned buffers, one thread
+// issues TMA tile loads (cp.async.bulk.tensor.3d) for a whole plane into an
+// S-deep ring completed through mbarriers (every wait bounded; a timeout
+// raises the plan's error flag and the CTA stops).  Otherwise the same ring is
+// filled with 4-byte cp.async copies (zero-filled outside the grid).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #include "native.cuh"
 
 namespace fdtd {
+namespace {
 
-// H (out of place), D, sources and E of one step.
+constexpr int FTX = 32;            // tile width in x (one warp)
+constexpr int MBAR_SPIN_LIMIT = 1 << 22;
+
+__host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) & ~127; }
+
+template <int TY>
+struct Geo {
+    static constexpr int EW = FTX + 8, EH = TY + 2;   // E^n box: x0-4 .. x0+TX+3, y0-1 .. y0+TY
+    static constexpr int HW = FTX + 4, HH = TY + 1;   // H box: x0-4 .. x0+TX-1, y0-1 .. y0+TY-1
+    static constexpr int E_BYTES = EW * EH * 4, H_BYTES = HW * HH * 4, T_BYTES = FTX * TY * 4, M_BYTES = FTX * TY;
+    static constexpr int OFF_E = 0;
+    static constexpr int OFF_H = OFF_E + 3 * pad128(E_BYTES);
+    static constexpr int OFF_T = OFF_H + 3 * pad128(H_BYTES);
+    static constexpr int OFF_M = OFF_T + 9 * pad128(T_BYTES);
+    static constexpr int STAGE = pad128(OFF_M + M_BYTES);
+    static constexpr int HNW = FTX + 1, HNH = TY + 1;  // H^{n+1/2} plane incl. low halo
+    static constexpr int HN_BYTES = pad128(3 * HNW * HNH * 4);
+    // expected transaction bytes per plane kind
+    static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 9u * T_BYTES + M_BYTES;
+    static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
+    static constexpr unsigned TX_EPI = 3u * E_BYTES;
+};
+
+// Tensor maps of one launch: E^n (3), H_old (3), D^n (3), D^{n-1} (3),
+// E^{n-1} (3), material (1).
+struct FusedMaps {
+    CUtensorMap m[16];
+};
+
+struct FusedArgs {
+    NativeConsts c;
+    int zchunk;
+};
+
+// ---------------------------------------------------------------- PTX helpers
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p)
+{
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: false after MBAR_SPIN_LIMIT polls.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
+{
+    for (int i = 0; i < MBAR_SPIN_LIMIT; i++)
+        if (mbar_try_wait(bar, parity))
+            return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, bool valid)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// ------------------------------------------------------------ plane staging
+
+enum PlaneKind { PLANE_FULL = 0, PLANE_PRO = 1, PLANE_EPI = 2 };
+
+template <int TY>
+__device__ __forceinline__ int plane_kind(int z, int zc0, int zc1)
+{
+    return z < zc0 ? PLANE_PRO : (z >= zc1 ? PLANE_EPI : PLANE_FULL);
+}
+
+// TMA: one thread arms the stage's barrier and issues the plane's boxes.
+template <int TY>
+__device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
+                                int z)
+{
+    using G = Geo<TY>;
+    const unsigned bytes = kind == PLANE_FULL ? G::TX_FULL : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI);
+    mbar_expect_tx(bar, bytes);
+    for (int c = 0; c < 3; c++)
+        tma_load_3d(smem_addr(stage + G::OFF_E + c * pad128(G::E_BYTES)), &maps.m[c], x0 - 4, y0 - 1, z, bar);
+    if (kind == PLANE_EPI)
+        return;
+    for (int c = 0; c < 3; c++)
+        tma_load_3d(smem_addr(stage + G::OFF_H + c * pad128(G::H_BYTES)), &maps.m[3 + c], x0 - 4, y0 - 1, z, bar);
+    if (kind == PLANE_PRO)
+        return;
+    for (int k = 0; k < 9; k++)
+        tma_load_3d(smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), &maps.m[6 + k], x0, y0, z, bar);
+    tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[15], x0, y0, z, bar);
+}
+
+// Generic: every thread copies part of each box with 4-byte cp.async
+// (zero-filled outside the grid); the material classes are read separately.
+template <int TY>
+__device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage, int kind, int x0, int y0, int z,
+                                    int tid)
+{
+    using G = Geo<TY>;
+    constexpr int NT = FTX * TY;
+    const int nx = c.nx, ny = c.ny;
+    const size_t plane = (size_t)nx * ny;
+    auto box = [&](const float *base, uint32_t dst, int xs, int ys, int w, int h) {
+        for (int i = tid; i < w * h; i += NT) {
+            const int gx = xs + i % w, gy = ys + i / w;
+            const bool ok = gx >= 0 && gx < nx && gy >= 0 && gy < ny;
+            const float *src = ok ? base + (size_t)z * plane + (size_t)gy * nx + gx : base;
+            cp_async4(dst + 4u * i, src, ok);
+        }
+    };
+    for (int k = 0; k < 3; k++)
+        box(c.e_cur[k], smem_addr(stage + G::OFF_E + k * pad128(G::E_BYTES)), x0 - 4, y0 - 1, G::EW, G::EH);
+    if (kind == PLANE_EPI)
+        return;
+    for (int k = 0; k < 3; k++)
+        box(c.h_in[k], smem_addr(stage + G::OFF_H + k * pad128(G::H_BYTES)), x0 - 4, y0 - 1, G::HW, G::HH);
+    if (kind == PLANE_PRO)
+        return;
+    const float *tiles[9] = {c.d_cur[0], c.d_cur[1], c.d_cur[2], c.d_prev[0], c.d_prev[1],
+                             c.d_prev[2], c.e_prev[0], c.e_prev[1], c.e_prev[2]};
+    for (int k = 0; k < 9; k++)
+        box(tiles[k], smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), x0, y0, FTX, TY);
+}
+
+// ---------------------------------------------------------------- the kernel
+
+template <int TY, int S, bool TMA>
+__global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
+                                                             const __grid_constant__ FusedMaps maps)
+{
+    using G = Geo<TY>;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // TMA destinations want 128-byte alignment; the launch adds 128 bytes of slack
+    unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    const NativeConsts &c = a.c;
+    const int nx = c.nx, ny = c.ny, nz = c.nz;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FTX + tx;
+    const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * TY;
+    const int x = x0 + tx, y = y0 + ty;
+    const int zc0 = blockIdx.z * a.zchunk, zc1 = min(nz, zc0 + a.zchunk);
+    const int p0 = max(zc0 - 1, 0), plast = min(zc1, nz - 1);
+    const int nplanes = plast - p0 + 1;
+
+    float *hn = reinterpret_cast<float *>(smem + S * G::STAGE);
+    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + c.nclasses * sizeof(DebyeCoef));
+    auto stage = [&](int k) { return smem + (k % S) * G::STAGE; };
+
+    // coefficient table -> shared memory
+    {
+        const float *src = reinterpret_cast<const float *>(c.coef);
+        float *dst = reinterpret_cast<float *>(coef);
+        for (int i = tid; i < c.nclasses * 8; i += FTX * TY)
+            dst[i] = src[i];
+    }
+    if (TMA && tid == 0) {
+        for (int s = 0; s < S; s++)
+            mbar_init(smem_addr(&bars[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // prologue: fill the ring
+    for (int k = 0; k < S; k++) {
+        if (k < nplanes) {
+            const int z = p0 + k;
+            if (TMA) {
+                if (tid == 0)
+                    issue_plane_tma<TY>(maps, stage(k), smem_addr(&bars[k % S]), plane_kind<TY>(z, zc0, zc1), x0, y0, z);
+            } else {
+                issue_plane_generic<TY>(c, stage(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z, tid);
+            }
+        }
+        if (!TMA)
+            cp_async_commit();
+    }
+
+    // source of this step (sample index n - n%3 in the reference scheme)
+    float jz_now = 0.0f;
+    if (c.nsources > 0) {
+        const int n = c.step_counter ? *c.step_counter : c.step;
+        const int j = c.scheme == FDTD_SCHEME_CORRECTED ? n : n - n % 3;
+        jz_now = (j >= 0 && j < c.njz) ? c.jz[j] : 0.0f;
+    }
+
+    const bool in_dom = x < nx && y < ny;
+    const size_t plane = (size_t)nx * ny;
+    const size_t col = (size_t)y * nx + x;
+    const float kx = c.kx, ky = c.ky, kz = c.kz, tcx = c.tx, tcy = c.ty, tcz = c.tz;
+    float hxm = 0.0f, hym = 0.0f;  // H^{n+1/2} of this column at z-1
+    uint8_t mat_next = 0;
+    if (!TMA && in_dom && zc0 < nz)
+        mat_next = c.mat[(size_t)zc0 * plane + col];
+
+    for (int k = 0; k < nplanes; k++) {
+        const int z = p0 + k;
+        if (z >= zc1)
+            break;
+        // planes k and k+1 resident
+        if (TMA) {
+            bool ok = true;
+            if (k == 0)
+                ok = mbar_wait(smem_addr(&bars[0]), 0);
+            if (ok && k + 1 < nplanes)
+                ok = mbar_wait(smem_addr(&bars[(k + 1) % S]), ((k + 1) / S) & 1);
+            // one decision for the whole CTA, so no thread is left at a barrier
+            if (__syncthreads_or(!ok)) {
+                if (tid == 0) {
+                    atomicExch(c.err, 1);
+                    // let the copies in flight land before the CTA exits (bounded)
+                    for (int j = k; j < nplanes && j < k + S; j++)
+                        mbar_wait(smem_addr(&bars[j % S]), (j / S) & 1);
+                }
+                __syncthreads();
+                return;
+            }
+        } else {
+            cp_async_wait<S - 2>();
+            __syncthreads();
+        }
+        const float *EA = reinterpret_cast<const float *>(stage(k) + G::OFF_E);
+        const float *EB = reinterpret_cast<const float *>(stage(k + 1) + G::OFF_E);
+        const float *HA = reinterpret_cast<const float *>(stage(k) + G::OFF_H);
+        constexpr int ES = pad128(G::E_BYTES) / 4, HS = pad128(G::H_BYTES) / 4, TS = pad128(G::T_BYTES) / 4;
+        auto ea = [&](int comp, int r, int cc) { return EA[comp * ES + r * G::EW + cc]; };
+        auto eb = [&](int comp, int r, int cc) { return EB[comp * ES + r * G::EW + cc]; };
+        auto ha = [&](int comp, int r, int cc) { return HA[comp * HS + r * G::HW + cc]; };
+        auto hnr = [&](int comp, int r, int cc) -> float & { return hn[(comp * G::HNH + r) * G::HNW + cc]; };
+
+        const bool zlo = z < nz - 1, zmid = z >= 1 && z < nz - 1;
+        // ---- H^{n+1/2} at plane z, own cell (fdtd_calculations.cu:43-76)
+        float hxn = 0.0f, hyn = 0.0f, hzn = 0.0f;
+        if (in_dom) {
+            const int r = ty + 1, cc = tx + 4;
+            const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
+            hxn = ha(0, r, cc);
+            hyn = ha(1, r, cc);
+            hzn = ha(2, r, cc);
+            if (x >= 1 && x < nx - 1 && y < ny - 1 && zlo)
+                hxn = hxn - ky * (ea(2, r + 1, cc) - ez_) + ky * (eb(1, r, cc) - ey_);
+            if (x < nx - 1 && y >= 1 && y < ny - 1 && zlo)
+                hyn = hyn - kz * (eb(0, r, cc) - ex_) + kx * (ea(2, r, cc + 1) - ez_);
+            if (x < nx - 1 && y < ny - 1 && zmid)
+                hzn = hzn - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+        }
+        if (z < zc0) {  // chunk prologue: only this column's H at zc0 - 1 is needed
+            hxm = hxn;
+            hym = hyn;
+        } else {
+            if (in_dom) {
+                hnr(0, ty + 1, tx + 1) = hxn;
+                hnr(1, ty + 1, tx + 1) = hyn;
+                hnr(2, ty + 1, tx + 1) = hzn;
+            }
+            // low-x halo column: hy, hz at x - 1
+            if (tx == 0 && x >= 1 && y < ny) {
+                const int r = ty + 1, cc = 3;  // x - 1
+                const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
+                const int xh = x - 1;
+                float v = ha(1, r, cc);
+                if (y >= 1 && y < ny - 1 && zlo)
+                    v = v - kz * (eb(0, r, cc) - ex_) + kx * (ea(2, r, cc + 1) - ez_);
+                hnr(1, ty + 1, 0) = v;
+                v = ha(2, r, cc);
+                if (xh < nx - 1 && y < ny - 1 && zmid)
+                    v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+                hnr(2, ty + 1, 0) = v;
+            }
+            // low-y halo row: hx, hz at y - 1
+            if (ty == 0 && y >= 1 && x < nx) {
+                const int r = 0, cc = tx + 4;  // y - 1
+                const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
+                float v = ha(0, r, cc);
+                if (x >= 1 && x < nx - 1 && zlo)
+                    v = v - ky * (ea(2, r + 1, cc) - ez_) + ky * (eb(1, r, cc) - ey_);
+                hnr(0, 0, tx + 1) = v;
+                v = ha(2, r, cc);
+                if (x < nx - 1 && zmid)
+                    v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+                hnr(2, 0, tx + 1) = v;
+            }
+            __syncthreads();
+
+            if (in_dom) {
+                const size_t i = (size_t)z * plane + col;
+                const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
+                const int t = ty * FTX + tx;
+                const float dn0 = T[0 * TS + t], dn1 = T[1 * TS + t], dn2 = T[2 * TS + t];
+                const float dp0 = T[3 * TS + t], dp1 = T[4 * TS + t], dp2 = T[5 * TS + t];
+                const float ep0 = T[6 * TS + t], ep1 = T[7 * TS + t], ep2 = T[8 * TS + t];
+                uint8_t cls;
+                if (TMA) {
+                    cls = (stage(k) + G::OFF_M)[t];
+                } else {
+                    cls = mat_next;
+                    if (z + 1 < zc1)
+                        mat_next = c.mat[i + plane];
+                }
+                // H^{n+1/2}: write the updated components
+                if (x >= 1 && x < nx - 1 && y < ny - 1 && zlo)
+                    c.h_out[0][i] = hxn;
+                if (x < nx - 1 && y >= 1 && y < ny - 1 && zlo)
+                    c.h_out[1][i] = hyn;
+                if (x < nx - 1 && y < ny - 1 && zmid)
+                    c.h_out[2][i] = hzn;
+
+                // ---- D^{n+1} (fdtd_calculations.cu:96-121) and sources (:198-211)
+                const bool xi = x >= 1 && x < nx - 1, yi = y >= 1 && y < ny - 1;
+                const bool dx_on = x < nx - 1 && yi && zmid;
+                const bool dy_on = xi && y < ny - 1 && zmid;
+                bool dz_on = xi && yi && zlo;
+                float d0 = dp0, d1 = dp1, d2 = dp2;
+                if (dx_on)
+                    d0 = dn0 + tcy * (hzn - hnr(2, ty, tx + 1)) - tcz * (hyn - hym);
+                if (dy_on)
+                    d1 = dn1 + tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
+                bool src = false;
+                for (int s = 0; s < c.nsources; s++)
+                    src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
+                if (dz_on || src) {
+                    d2 = dn2 + tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
+                    if (src)
+                        d2 = d2 - jz_now;
+                    dz_on = true;
+                }
+                if (dx_on) c.d_prev[0][i] = d0;
+                if (dy_on) c.d_prev[1][i] = d1;
+                if (dz_on) c.d_prev[2][i] = d2;
+
+                // ---- Debye E^{n+1} (fdtd_calculations.cu:146-183)
+                const bool ex_on = x < nx - 1 && yi && zmid;
+                const bool eyz_on = x >= 1 && z >= 1;
+                if (ex_on || eyz_on) {
+                    const DebyeCoef kc = coef[cls];
+                    const int r = ty + 1, cc = tx + 4;
+                    if (ex_on)
+                        c.e_prev[0][i] = debye_update(kc, ea(0, r, cc), ep0, d0, dn0, dp0);
+                    if (eyz_on) {
+                        c.e_prev[1][i] = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
+                        c.e_prev[2][i] = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
+                    }
+                }
+            }
+            hxm = hxn;
+            hym = hyn;
+        }
+        __syncthreads();  // stage k and hn fully consumed
+        // refill the stage of plane k with plane k + S
+        const int kn = k + S;
+        if (TMA) {
+            if (tid == 0 && kn < nplanes) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const int zn = p0 + kn;
+                issue_plane_tma<TY>(maps, stage(kn), smem_addr(&bars[kn % S]), plane_kind<TY>(zn, zc0, zc1), x0, y0,
+                                    zn);
+            }
+        } else {
+            if (kn < nplanes) {
+                const int zn = p0 + kn;
+                issue_plane_generic<TY>(c, stage(kn), plane_kind<TY>(zn, zc0, zc1), x0, y0, zn, tid);
+            }
+            cp_async_commit();
+        }
+    }
+    if (!TMA)
+        cp_async_wait<0>();
+}
+
+// ------------------------------------------------------------------ host side
+
+constexpr int TY_SEL = 8;
+constexpr int S_SEL = 3;
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    });
+    return fn;
+}
+
+bool encode_map(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void *base, bool is_u8, int nx, int ny,
+                int nz, int bx, int by)
+{
+    const size_t es = is_u8 ? 1 : 4;
+    cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    cuuint64_t strides[2] = {(cuuint64_t)(nx * es), (cuuint64_t)((size_t)nx * ny * es)};
+    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r =
+        fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base),
+           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+template <bool TMA>
+int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
+{
+    using G = Geo<TY_SEL>;
+    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA>;
+    const int smem = 128 + S_SEL * G::STAGE + G::HN_BYTES + a.c.nclasses * (int)sizeof(DebyeCoef) + S_SEL * 8;
+    static std::once_flag once;
+    std::call_once(once, [&] {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             128 + S_SEL * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) +
+                                 S_SEL * 8);
+    });
+    const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
+    kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(a, maps);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? FDTD_OK : (int)e;
+}
+
+}  // namespace
+
+int fused_zchunk(int nz)
+{
+    // about 64 planes per CTA: enough CTAs per wave on 152 SMs, little
+    // prologue/epilogue traffic at chunk borders
+    const int chunks = (nz + 63) / 64;
+    return (nz + chunks - 1) / chunks;
+}
+
+bool fused_uses_tma(const NativeConsts &c)
+{
+    if (c.nx % 16 != 0 || !encode_fn())
+        return false;
+    for (int k = 0; k < 3; k++)
+        if (!aligned16(c.e_cur[k]) || !aligned16(c.h_in[k]) || !aligned16(c.d_cur[k]) || !aligned16(c.d_prev[k]) ||
+            !aligned16(c.e_prev[k]))
+            return false;
+    return aligned16(c.mat);
+}
+
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
 {
-    int st = launch_h(c, s);
-    if (st == FDTD_OK)
-        st = launch_de(c, s);
-    return st;
+    FusedArgs a;
+    a.c = c;
+    const char *env = getenv("FDTD_ZCHUNK");
+    a.zchunk = env ? atoi(env) : fused_zchunk(c.nz);
+    if (a.zchunk < 1)
+        a.zchunk = c.nz;
+    FusedMaps maps;
+    memset(&maps, 0, sizeof maps);
+    if (fused_uses_tma(c)) {
+        auto fn = encode_fn();
+        using G = Geo<TY_SEL>;
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; k++) {
+            ok &= encode_map(fn, &maps.m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, G::EW, G::EH);
+            ok &= encode_map(fn, &maps.m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, G::HW, G::HH);
+            ok &= encode_map(fn, &maps.m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+        }
+        ok &= encode_map(fn, &maps.m[15], c.mat, true, c.nx, c.ny, c.nz, FTX, TY_SEL);
+        if (ok)
+            return launch_fused_impl<true>(a, maps, s);
+    }
+    return launch_fused_impl<false>(a, maps, s);
 }
 
 int launch_step(const NativeConsts &c, cudaStream_t s)

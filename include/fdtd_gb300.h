@@ -36,7 +36,8 @@ enum fdtd_status_code {
     FDTD_ERR_FORMAT = 10003,      /* an input file does not follow the reference format */
     FDTD_ERR_NO_SYMBOLS = 10004,  /* a compat launcher ran before fdtd_copy_symbols on this device */
     FDTD_ERR_NOMEM = 10005,       /* a host allocation failed */
-    FDTD_ERR_STATE = 10006        /* call not valid in the object's current state */
+    FDTD_ERR_STATE = 10006,       /* call not valid in the object's current state */
+    FDTD_ERR_DEVICE_TIMEOUT = 10007 /* a kernel's bounded wait gave up; its results are invalid */
 };
 
 /* Human-readable text for any status this library returns. */
@@ -216,6 +217,10 @@ typedef struct fdtd_plan fdtd_plan;
 int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int scheme,
                      const float *const rp_host[6], fdtd_plan **out);
 int fdtd_plan_destroy(fdtd_plan *plan);
+
+/* Synchronises the device and reports (then clears) the plan's error flag:
+ * FDTD_ERR_DEVICE_TIMEOUT if a kernel gave up a bounded wait. */
+int fdtd_plan_status(fdtd_plan *plan);
 
 /* Device state of the native path.  E and D keep two slots each: the
  * "prev" slot holds step n-1 on entry and receives step n+1. */

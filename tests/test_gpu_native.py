@@ -67,3 +67,33 @@ def test_single_pass_rejects_in_place_h(cuda):
     f = st.fields(0, single_pass=False)  # H in place
     assert fg.lib().fdtd_step(plan.handle, C.byref(f), 0, None) == fg.FDTD_ERR_INVALID
     plan.close()
+
+
+@pytest.mark.parametrize("dims,seed", [((48, 20, 70), 5), ((32, 8, 130), 6), ((64, 64, 64), 8), ((96, 7, 9), 9)])
+def test_single_pass_tma_path_and_chunk_borders(cuda, dims, seed):
+    """nx a multiple of 16 selects the TMA staging; nz > 64 splits z into
+    chunks whose first plane recomputes H of the plane below."""
+    nx, ny, nz = dims
+    codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, seed, nsrc=4)
+    steps = 9
+    media = class_media(codes, specs, rp)
+    st = po.State(nx, ny, nz, np.float32)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts), media, st, 0, steps)
+    raw = make_params(dims, consts, sources, jz)
+    got = run_native(cuda, raw, specs, codes, rp, steps, mode="single")
+    assert_fields_close(got, st.latest(steps))
+
+
+@pytest.mark.parametrize("chunk", [1, 2, 5])
+@pytest.mark.parametrize("dims", [(32, 16, 23), (37, 11, 17)])
+def test_single_pass_small_z_chunks(cuda, monkeypatch, dims, chunk):
+    monkeypatch.setenv("FDTD_ZCHUNK", str(chunk))
+    nx, ny, nz = dims
+    codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, 10 + chunk, nsrc=3)
+    steps = 8
+    media = class_media(codes, specs, rp)
+    st = po.State(nx, ny, nz, np.float32)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts), media, st, 0, steps)
+    raw = make_params(dims, consts, sources, jz)
+    got = run_native(cuda, raw, specs, codes, rp, steps, mode="single")
+    assert_fields_close(got, st.latest(steps))
