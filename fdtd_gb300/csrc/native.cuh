@@ -20,6 +20,7 @@ struct fdtd_plan {
     float *d_jz = nullptr;                // FDTD_JZ_LEN entries
     fdtd::MurSlabs rp{};                  // six Mur slabs
     int *d_err = nullptr;                 // device error flag
+    int *d_done = nullptr;                // fused-kernel CTA completion counter
 };
 
 namespace fdtd {
@@ -42,6 +43,7 @@ struct NativeConsts {
     int step;              // step index n when step_counter is null
     int *step_counter;     // device step index (graph replay), may be null
     int *err;              // device error flag (a bounded wait gave up)
+    int *done;             // CTA completion counter of the fused kernel
     const float *h_in[3];
     float *h_out[3];
     const float *e_cur[3];
@@ -65,7 +67,7 @@ struct StepKernel {
     const char *name;
     int (*launch)(const NativeConsts &, cudaStream_t);
 };
-int step_kernels(int kernel_kind, StepKernel *out, int max);
+int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int max);
 
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);

@@ -511,7 +511,8 @@ int fdtd_solver_profile(fdtd_solver *s, int nsteps, float *avg_ms, int max_kerne
         s->copy_pending = false;
     }
     StepKernel ks[8];
-    const int nk = step_kernels(s->kernel, ks, 8);
+    const fdtd_native_fields f0 = step_fields(s, s->steps);
+    const int nk = step_kernels(s->kernel, make_consts(s->plan, &f0, s->steps), ks, 8);
     std::vector<cudaEvent_t> ev((size_t)nsteps * (nk + 1), nullptr);
     for (auto &e : ev)
         if (st == FDTD_OK)
@@ -555,7 +556,8 @@ const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k)
     if (!s || k < 0)
         return nullptr;
     StepKernel ks[8];
-    const int nk = step_kernels(s->kernel, ks, 8);
+    const fdtd_native_fields f0 = step_fields(s, s->steps);
+    const int nk = step_kernels(s->kernel, make_consts(s->plan, &f0, s->steps), ks, 8);
     return k < nk ? ks[k].name : nullptr;
 }
 

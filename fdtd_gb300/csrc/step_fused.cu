@@ -42,6 +42,7 @@ struct Geo {
     static constexpr int STAGE = pad128(OFF_M + M_BYTES);
     static constexpr int HNW = FTX + 1, HNH = TY + 1;  // H^{n+1/2} plane incl. low halo
     static constexpr int HN_BYTES = pad128(3 * HNW * HNH * 4);
+    static constexpr int XCHG_BYTES = pad128(3 * FTX * TY * 4);  // E^{n+1} of the tile (Mur faces)
     // expected transaction bytes per plane kind
     static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 9u * T_BYTES + M_BYTES;
     static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
@@ -57,6 +58,9 @@ struct FusedMaps {
 struct FusedArgs {
     NativeConsts c;
     int zchunk;
+    int fuse_mur;          // Mur faces inside this kernel (else a separate launch)
+    int *done;             // CTA completion counter (step counter advance)
+    unsigned total_ctas;
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -113,6 +117,21 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Step counter advance: the last CTA of the launch to finish increments it
+// (every CTA read it at its start, before its own increment of `done`).
+__device__ __forceinline__ void finish_cta(const NativeConsts &c, int fuse_mur, int *done, unsigned total)
+{
+    if (!fuse_mur || !done || !c.step_counter)
+        return;
+    __threadfence();
+    const unsigned prev = atomicAdd(reinterpret_cast<unsigned *>(done), 1u);
+    if (prev == total - 1) {
+        atomicExch(done, 0);
+        __threadfence();
+        atomicAdd(c.step_counter, 1);
+    }
+}
 
 // ------------------------------------------------------------ plane staging
 
@@ -197,8 +216,9 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     const int nplanes = plast - p0 + 1;
 
     float *hn = reinterpret_cast<float *>(smem + S * G::STAGE);
-    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + c.nclasses * sizeof(DebyeCoef));
+    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES + G::XCHG_BYTES);
+    uint64_t *bars =
+        reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + G::XCHG_BYTES + c.nclasses * sizeof(DebyeCoef));
     auto stage = [&](int k) { return smem + (k % S) * G::STAGE; };
 
     // coefficient table -> shared memory
@@ -243,6 +263,10 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     const size_t col = (size_t)y * nx + x;
     const float kx = c.kx, ky = c.ky, kz = c.kz, tcx = c.tx, tcy = c.ty, tcz = c.tz;
     float hxm = 0.0f, hym = 0.0f;  // H^{n+1/2} of this column at z-1
+    // E^{n+1} (before face values) and E^n of this column at z-1, for the z faces
+    float en_prev0 = 0.0f, en_prev1 = 0.0f, e_prev_n0 = 0.0f, e_prev_n1 = 0.0f;
+    const bool boundary_cta = x0 == 0 || x0 + FTX >= nx || y0 == 0 || y0 + TY >= ny;
+    float *xchg = reinterpret_cast<float *>(smem + S * G::STAGE + G::HN_BYTES);
     uint8_t mat_next = 0;
     if (!TMA && in_dom && zc0 < nz)
         mat_next = c.mat[(size_t)zc0 * plane + col];
@@ -265,6 +289,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                     // let the copies in flight land before the CTA exits (bounded)
                     for (int j = k; j < nplanes && j < k + S; j++)
                         mbar_wait(smem_addr(&bars[j % S]), (j / S) & 1);
+                    finish_cta(c, a.fuse_mur, a.done, a.total_ctas);
                 }
                 __syncthreads();
                 return;
@@ -302,6 +327,10 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             hxm = hxn;
             hym = hyn;
         } else {
+            if (z == 0 && in_dom) {  // E^n of plane 0 for the near z face
+                e_prev_n0 = ea(0, ty + 1, tx + 4);
+                e_prev_n1 = ea(1, ty + 1, tx + 4);
+            }
             if (in_dom) {
                 hnr(0, ty + 1, tx + 1) = hxn;
                 hnr(1, ty + 1, tx + 1) = hyn;
@@ -336,8 +365,11 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             }
             __syncthreads();
 
+            const size_t i = (size_t)z * plane + col;
+            const int r = ty + 1, cc = tx + 4;
+            float en0 = 0.0f, en1 = 0.0f, en2 = 0.0f;  // E^{n+1}: the slot's value unless updated
+            bool w0 = false, w1 = false, w2 = false;
             if (in_dom) {
-                const size_t i = (size_t)z * plane + col;
                 const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
                 const int t = ty * FTX + tx;
                 const float dn0 = T[0 * TS + t], dn1 = T[1 * TS + t], dn2 = T[2 * TS + t];
@@ -383,18 +415,117 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                 if (dz_on) c.d_prev[2][i] = d2;
 
                 // ---- Debye E^{n+1} (fdtd_calculations.cu:146-183)
-                const bool ex_on = x < nx - 1 && yi && zmid;
-                const bool eyz_on = x >= 1 && z >= 1;
-                if (ex_on || eyz_on) {
+                w0 = x < nx - 1 && yi && zmid;
+                w1 = w2 = x >= 1 && z >= 1;
+                en0 = ep0;
+                en1 = ep1;
+                en2 = ep2;
+                if (w0 || w1) {
                     const DebyeCoef kc = coef[cls];
-                    const int r = ty + 1, cc = tx + 4;
-                    if (ex_on)
-                        c.e_prev[0][i] = debye_update(kc, ea(0, r, cc), ep0, d0, dn0, dp0);
-                    if (eyz_on) {
-                        c.e_prev[1][i] = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
-                        c.e_prev[2][i] = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
+                    if (w0)
+                        en0 = debye_update(kc, ea(0, r, cc), ep0, d0, dn0, dp0);
+                    if (w1) {
+                        en1 = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
+                        en2 = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
                     }
                 }
+            }
+
+            // ---- Mur faces (fdtd_calculations.cu:216-428), when fused
+            if (a.fuse_mur) {
+                const float dt = c.dt, me = c.me;
+                const bool fix = c.scheme == FDTD_SCHEME_CORRECTED;
+                const float pre0 = en0, pre1 = en1;  // E^{n+1} before any face value
+                if (boundary_cta) {
+                    if (in_dom) {
+                        xchg[(0 * TY + ty) * FTX + tx] = en0;
+                        xchg[(1 * TY + ty) * FTX + tx] = en1;
+                        xchg[(2 * TY + ty) * FTX + tx] = en2;
+                    }
+                    __syncthreads();
+                    if (in_dom) {
+                        auto xg = [&](int comp, int yy, int xx) { return xchg[(comp * TY + yy) * FTX + xx]; };
+                        const bool zm = z >= 1 && z < nz - 1, zl = z < nz - 1;
+                        if (x == 0) {
+                            const size_t b = ((size_t)z * ny + y) * 2;
+                            const float rs = c.rp.rpx0[b], rn = c.rp.rpx0[b + 1];
+                            if (y < ny - 1 && zm) {
+                                en1 = mur_value(dt, c.hx, me, rs, rn, xg(1, ty, tx + 1), ea(1, r, cc + 1), ea(1, r, cc));
+                                w1 = true;
+                            }
+                            if (y >= 1 && y < ny - 1 && zl) {
+                                en2 = mur_value(dt, c.hx, me, rs, rn, xg(2, ty, tx + 1), ea(2, r, cc + 1), ea(2, r, cc));
+                                w2 = true;
+                            }
+                        } else if (x == nx - 1) {
+                            const size_t b = ((size_t)z * ny + y) * 2;
+                            const float rs = c.rp.rpx_end[b + 1], rn = c.rp.rpx_end[b];
+                            if (y < ny - 1 && zm) {
+                                // the reference reads E^n at x-1 in the first term here (:323)
+                                const float t1 = fix ? xg(1, ty, tx - 1) : ea(1, r, cc - 1);
+                                en1 = mur_value(dt, c.hx, me, rs, rn, t1, ea(1, r, cc - 1), ea(1, r, cc));
+                                w1 = true;
+                            }
+                            if (y >= 1 && y < ny - 1 && zl) {
+                                en2 = mur_value(dt, c.hx, me, rs, rn, xg(2, ty, tx - 1), ea(2, r, cc - 1), ea(2, r, cc));
+                                w2 = true;
+                            }
+                        }
+                        if (y == 0) {
+                            const float rs = c.rp.rpy0[((size_t)z * 2 + 0) * nx + x];
+                            const float rn = c.rp.rpy0[((size_t)z * 2 + 1) * nx + x];
+                            if (x < nx - 1 && zm) {
+                                en0 = mur_value(dt, c.hy, me, rs, rn, xg(0, ty + 1, tx), ea(0, r + 1, cc), ea(0, r, cc));
+                                w0 = true;
+                            }
+                            if (x >= 1 && x < nx - 1 && zl) {
+                                en2 = mur_value(dt, c.hy, me, rs, rn, xg(2, ty + 1, tx), ea(2, r + 1, cc), ea(2, r, cc));
+                                w2 = true;
+                            }
+                        } else if (y == ny - 1) {
+                            const float rs = c.rp.rpy_end[((size_t)z * 2 + 1) * nx + x];
+                            const float rn = c.rp.rpy_end[((size_t)z * 2 + 0) * nx + x];
+                            if (x < nx - 1 && zm) {
+                                en0 = mur_value(dt, c.hy, me, rs, rn, xg(0, ty - 1, tx), ea(0, r - 1, cc), ea(0, r, cc));
+                                w0 = true;
+                            }
+                            if (x >= 1 && x < nx - 1 && zl) {
+                                en2 = mur_value(dt, c.hy, me, rs, rn, xg(2, ty - 1, tx), ea(2, r - 1, cc), ea(2, r, cc));
+                                w2 = true;
+                            }
+                        }
+                    }
+                }
+                if (in_dom) {
+                    const size_t pz = (size_t)y * nx + x;
+                    if (z == nz - 1) {  // far z face from the plane below, kept in registers
+                        const float rs = c.rp.rpz_end[(size_t)1 * plane + pz], rn = c.rp.rpz_end[pz];
+                        if (x < nx - 1 && y >= 1 && y < ny - 1) {
+                            en0 = mur_value(dt, c.hz, me, rs, rn, en_prev0, e_prev_n0, ea(0, r, cc));
+                            w0 = true;
+                        }
+                        if (x >= 1 && x < nx - 1 && y < ny - 1) {
+                            en1 = mur_value(dt, c.hz, me, rs, rn, en_prev1, e_prev_n1, ea(1, r, cc));
+                            w1 = true;
+                        }
+                    }
+                    if (z == 1) {  // near z face (plane 0), one plane late
+                        const float rs = c.rp.rpz0[pz], rn = c.rp.rpz0[(size_t)1 * plane + pz];
+                        if (x < nx - 1 && y >= 1 && y < ny - 1)
+                            c.e_prev[0][pz] = mur_value(dt, c.hz, me, rs, rn, pre0, ea(0, r, cc), e_prev_n0);
+                        if (x >= 1 && x < nx - 1 && y < ny - 1)
+                            c.e_prev[1][pz] = mur_value(dt, c.hz, me, rs, rn, pre1, ea(1, r, cc), e_prev_n1);
+                    }
+                    en_prev0 = pre0;
+                    en_prev1 = pre1;
+                    e_prev_n0 = ea(0, r, cc);
+                    e_prev_n1 = ea(1, r, cc);
+                }
+            }
+            if (in_dom) {
+                if (w0) c.e_prev[0][i] = en0;
+                if (w1) c.e_prev[1][i] = en1;
+                if (w2) c.e_prev[2][i] = en2;
             }
             hxm = hxn;
             hym = hyn;
@@ -419,6 +550,9 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     }
     if (!TMA)
         cp_async_wait<0>();
+    __syncthreads();
+    if (tid == 0)
+        finish_cta(c, a.fuse_mur, a.done, a.total_ctas);
 }
 
 // ------------------------------------------------------------------ host side
@@ -463,15 +597,18 @@ int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
     using G = Geo<TY_SEL>;
     auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA>;
-    const int smem = 128 + S_SEL * G::STAGE + G::HN_BYTES + a.c.nclasses * (int)sizeof(DebyeCoef) + S_SEL * 8;
+    const int smem =
+        128 + S_SEL * G::STAGE + G::HN_BYTES + G::XCHG_BYTES + a.c.nclasses * (int)sizeof(DebyeCoef) + S_SEL * 8;
     static std::once_flag once;
     std::call_once(once, [&] {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             128 + S_SEL * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) +
-                                 S_SEL * 8);
+                             128 + S_SEL * G::STAGE + G::HN_BYTES + G::XCHG_BYTES +
+                                 FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) + S_SEL * 8);
     });
     const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
-    kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(a, maps);
+    FusedArgs b = a;
+    b.total_ctas = grid.x * grid.y * grid.z;
+    kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(b, maps);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FDTD_OK : (int)e;
 }
@@ -484,6 +621,26 @@ int fused_zchunk(int nz)
     // prologue/epilogue traffic at chunk borders
     const int chunks = (nz + 63) / 64;
     return (nz + chunks - 1) / chunks;
+}
+
+int fused_zchunk_for(const NativeConsts &c)
+{
+    const char *env = getenv("FDTD_ZCHUNK");
+    int z = env ? atoi(env) : fused_zchunk(c.nz);
+    return z < 1 ? c.nz : z;
+}
+
+// Mur faces can be computed inside the fused kernel when every face cell's
+// inner neighbour lies in the same CTA: the last x tile and the last y tile
+// hold at least two columns/rows and the first and last z chunks at least two
+// planes.  Otherwise the separate face kernel runs after it.
+bool fused_mur_ok(const NativeConsts &c)
+{
+    if (getenv("FDTD_SEPARATE_MUR"))
+        return false;
+    const int zc = fused_zchunk_for(c);
+    const int last = c.nz - ((c.nz - 1) / zc) * zc;
+    return zc >= 2 && last >= 2 && c.nx % FTX != 1 && c.ny % TY_SEL != 1;
 }
 
 bool fused_uses_tma(const NativeConsts &c)
@@ -501,10 +658,10 @@ int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
 {
     FusedArgs a;
     a.c = c;
-    const char *env = getenv("FDTD_ZCHUNK");
-    a.zchunk = env ? atoi(env) : fused_zchunk(c.nz);
-    if (a.zchunk < 1)
-        a.zchunk = c.nz;
+    a.zchunk = fused_zchunk_for(c);
+    a.fuse_mur = fused_mur_ok(c) ? 1 : 0;
+    a.done = c.done;
+    a.total_ctas = 0;
     FusedMaps maps;
     memset(&maps, 0, sizeof maps);
     if (fused_uses_tma(c)) {
@@ -528,17 +685,19 @@ int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
 int launch_step(const NativeConsts &c, cudaStream_t s)
 {
     int st = launch_h_de_fused(c, s);
-    if (st == FDTD_OK)
+    if (st == FDTD_OK && !fused_mur_ok(c))
         st = launch_mur(c, s);
     return st;
 }
 
-int step_kernels(int kernel_kind, StepKernel *out, int max)
+int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int max)
 {
     StepKernel single[] = {{"fused_step", launch_h_de_fused}, {"mur", launch_mur}};
     StepKernel two[] = {{"h", launch_h}, {"de", launch_de}, {"mur", launch_mur}};
     const StepKernel *src = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? single : two;
-    const int n = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? 2 : 3;
+    int n = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? 2 : 3;
+    if (kernel_kind == FDTD_KERNEL_SINGLE_PASS && fused_mur_ok(c))
+        n = 1;
     for (int k = 0; k < n && k < max; k++)
         out[k] = src[k];
     return n;

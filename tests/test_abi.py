@@ -44,3 +44,13 @@ def test_invalid_arguments_return_status_without_a_gpu():
     assert L.fdtd_plan_create(None, None, 0, 0, None, None) == fg.FDTD_ERR_INVALID
     assert L.fdtd_solver_create(None, None) == fg.FDTD_ERR_INVALID
     assert L.fdtd_step(None, None, 0, None) == fg.FDTD_ERR_INVALID
+
+
+def test_drop_in_executable_built_and_reports_usage():
+    import subprocess
+
+    assert fg.EXE_PATH.exists()
+    r = subprocess.run([str(fg.EXE_PATH), "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+    r = subprocess.run([str(fg.EXE_PATH), "--params", "/nonexistent/input_params"], capture_output=True, text=True)
+    assert r.returncode == 1 and "failed" in r.stderr

@@ -115,3 +115,28 @@ def test_c1_sphere_reference_scheme_finite_window(cuda, tmp_path):
     want = st.latest(60)
     assert all(np.all(np.isfinite(v)) for v in want.values())
     assert_fields_close(got, want)
+
+
+def test_drop_in_executable_writes_reference_layout(cuda, tmp_path):
+    """fdtd_gb300/bin/fdtd reads input_params / mat_specs / PGM slices like the
+    reference program and writes every field every step (writeResults3d
+    layout); its Ez after the last step equals the solver's."""
+    import subprocess
+
+    n = 12
+    path = ph.c1_inputs(tmp_path, n=n, t_max=3)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(fg.EXE_PATH), "--params", str(path), "--specs", str(tmp_path / "mat_specs")],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    names = sorted(q.name for q in out.iterdir())
+    assert len(names) == 3 * 9 * n  # 3 steps, 9 fields, n planes
+    p, codes, specs, s = solver_from_files(tmp_path / "again", n, 3, fg.KERNEL_SINGLE_PASS)
+    s.run(3)
+    ez = s.field("ez")
+    s.close()
+    for z in (0, 5, n - 1):
+        text = (out / f"E_field_z_00002_z{z:05d}.out").read_text()
+        want = "".join("".join(" % 9.3E" % float(v) for v in row) + "\n" for row in ez[z])
+        assert text == want
