@@ -100,8 +100,8 @@ struct MurSlabs {
 // eT: E^{n+1} (written), eS: E^n.  fix_ey selects the corrected scheme's
 // E^{n+1} term on the ey x = nx-1 face (the reference reads E^n there, :323).
 __device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny, int nz, float dt, float hx, float hy,
-                                          float hz, float me, const MurSlabs &rp, float *const eT[3],
-                                          const float *const eS[3], bool fix_ey)
+                                          float hz, float me, const MurSlabs &rp, float *t0, float *t1, float *t2,
+                                          const float *s0, const float *s1, const float *s2, bool fix_ey)
 {
     const MurFace m = mur_face(f, nx, ny, nz);
     if (iu >= m.len_u || iv >= m.len_v)
@@ -128,8 +128,9 @@ __device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny,
     }
     const size_t i = cell_index(x, y, z, nx, ny);
     const size_t j = cell_index(x + dxn, y + dyn, z + dzn, nx, ny);
-    const float *S = eS[m.comp];
-    float *T = eT[m.comp];
+    // component pointers picked with selects (an indexed array would live in local memory)
+    const float *S = m.comp == 0 ? s0 : (m.comp == 1 ? s1 : s2);
+    float *T = m.comp == 0 ? t0 : (m.comp == 1 ? t1 : t2);
     // fdtd_calculations.cu:323: the ey face at x = nx-1 reads E^n at x-1 in
     // its first term as well.
     const bool quirk = m.comp == 1 && m.axis == 0 && m.far && !fix_ey;

@@ -204,10 +204,9 @@ __global__ void __launch_bounds__(256) native_mur_kernel(NativeConsts c)
         atomicAdd(c.step_counter, 1);
     if (idx >= (long long)m.len_u * m.len_v)
         return;
-    float *eT[3] = {c.e_prev[0], c.e_prev[1], c.e_prev[2]};
-    const float *eS[3] = {c.e_cur[0], c.e_cur[1], c.e_cur[2]};
-    mur_apply(f, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.dt, c.hx, c.hy, c.hz, c.me, c.rp, eT,
-              eS, c.scheme == FDTD_SCHEME_CORRECTED);
+    mur_apply(f, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.dt, c.hx, c.hy, c.hz, c.me, c.rp,
+              c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
+              c.scheme == FDTD_SCHEME_CORRECTED);
 }
 
 int launch_status()

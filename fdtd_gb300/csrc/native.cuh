@@ -69,6 +69,11 @@ struct StepKernel {
 };
 int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int max);
 
+// H, D, sources and E of one step in the single-pass kernel (Mur faces
+// included when fused_mur_ok).
+int launch_h_de_fused(const NativeConsts &c, cudaStream_t s);
+bool fused_mur_ok(const NativeConsts &c);
+
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);
 

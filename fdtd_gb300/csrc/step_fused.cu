@@ -143,25 +143,28 @@ __device__ __forceinline__ int plane_kind(int z, int zc0, int zc1)
     return z < zc0 ? PLANE_PRO : (z >= zc1 ? PLANE_EPI : PLANE_FULL);
 }
 
-// TMA: one thread arms the stage's barrier and issues the plane's boxes.
+// TMA: lane 0 of warp 0 arms the stage's barrier, then lane b issues box b
+// (3 E^n boxes, 3 H boxes, 9 tile boxes, 1 class box), so the 16 copies of a
+// plane leave in one warp instruction instead of sixteen.
 template <int TY>
 __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
-                                int z)
+                                int z, int lane)
 {
     using G = Geo<TY>;
     const unsigned bytes = kind == PLANE_FULL ? G::TX_FULL : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI);
-    mbar_expect_tx(bar, bytes);
-    for (int c = 0; c < 3; c++)
-        tma_load_3d(smem_addr(stage + G::OFF_E + c * pad128(G::E_BYTES)), &maps.m[c], x0 - 4, y0 - 1, z, bar);
-    if (kind == PLANE_EPI)
-        return;
-    for (int c = 0; c < 3; c++)
-        tma_load_3d(smem_addr(stage + G::OFF_H + c * pad128(G::H_BYTES)), &maps.m[3 + c], x0 - 4, y0 - 1, z, bar);
-    if (kind == PLANE_PRO)
-        return;
-    for (int k = 0; k < 9; k++)
-        tma_load_3d(smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), &maps.m[6 + k], x0, y0, z, bar);
-    tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[15], x0, y0, z, bar);
+    const int nbox = kind == PLANE_FULL ? 16 : (kind == PLANE_PRO ? 6 : 3);
+    if (lane == 0)
+        mbar_expect_tx(bar, bytes);
+    __syncwarp();
+    if (lane < 3)
+        tma_load_3d(smem_addr(stage + G::OFF_E + lane * pad128(G::E_BYTES)), &maps.m[lane], x0 - 4, y0 - 1, z, bar);
+    else if (lane < 6 && lane < nbox)
+        tma_load_3d(smem_addr(stage + G::OFF_H + (lane - 3) * pad128(G::H_BYTES)), &maps.m[lane], x0 - 4, y0 - 1, z,
+                    bar);
+    else if (lane < 15 && lane < nbox)
+        tma_load_3d(smem_addr(stage + G::OFF_T + (lane - 6) * pad128(G::T_BYTES)), &maps.m[lane], x0, y0, z, bar);
+    else if (lane == 15 && lane < nbox)
+        tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[15], x0, y0, z, bar);
 }
 
 // Generic: every thread copies part of each box with 4-byte cp.async
@@ -198,7 +201,7 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
 
 // ---------------------------------------------------------------- the kernel
 
-template <int TY, int S, bool TMA>
+template <int TY, int S, bool TMA, bool MUR>
 __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
                                                              const __grid_constant__ FusedMaps maps)
 {
@@ -216,9 +219,9 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     const int nplanes = plast - p0 + 1;
 
     float *hn = reinterpret_cast<float *>(smem + S * G::STAGE);
-    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES + G::XCHG_BYTES);
-    uint64_t *bars =
-        reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + G::XCHG_BYTES + c.nclasses * sizeof(DebyeCoef));
+    constexpr int XB = MUR ? G::XCHG_BYTES : 0;
+    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES + XB);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + XB + c.nclasses * sizeof(DebyeCoef));
     auto stage = [&](int k) { return smem + (k % S) * G::STAGE; };
 
     // coefficient table -> shared memory
@@ -240,8 +243,9 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         if (k < nplanes) {
             const int z = p0 + k;
             if (TMA) {
-                if (tid == 0)
-                    issue_plane_tma<TY>(maps, stage(k), smem_addr(&bars[k % S]), plane_kind<TY>(z, zc0, zc1), x0, y0, z);
+                if (tid < 32)
+                    issue_plane_tma<TY>(maps, stage(k), smem_addr(&bars[k % S]), plane_kind<TY>(z, zc0, zc1), x0, y0, z,
+                                        tid);
             } else {
                 issue_plane_generic<TY>(c, stage(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z, tid);
             }
@@ -289,7 +293,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                     // let the copies in flight land before the CTA exits (bounded)
                     for (int j = k; j < nplanes && j < k + S; j++)
                         mbar_wait(smem_addr(&bars[j % S]), (j / S) & 1);
-                    finish_cta(c, a.fuse_mur, a.done, a.total_ctas);
+                    finish_cta(c, MUR, a.done, a.total_ctas);
                 }
                 __syncthreads();
                 return;
@@ -308,6 +312,27 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         auto hnr = [&](int comp, int r, int cc) -> float & { return hn[(comp * G::HNH + r) * G::HNW + cc]; };
 
         const bool zlo = z < nz - 1, zmid = z >= 1 && z < nz - 1;
+        // Mur slab values this thread's face cells need on this plane, loaded
+        // early so their latency overlaps the H, D and E work
+        float rxs = 0.0f, rxn = 0.0f, rys = 0.0f, ryn = 0.0f, rzs = 0.0f, rzn = 0.0f;
+        if (MUR && in_dom && z >= zc0) {
+            if (x == 0 || x == nx - 1) {
+                const float *slab = x == 0 ? c.rp.rpx0 : c.rp.rpx_end;
+                const size_t b = ((size_t)z * ny + y) * 2;
+                rxs = slab[b + (x == 0 ? 0 : 1)];
+                rxn = slab[b + (x == 0 ? 1 : 0)];
+            }
+            if (y == 0 || y == ny - 1) {
+                const float *slab = y == 0 ? c.rp.rpy0 : c.rp.rpy_end;
+                rys = slab[((size_t)z * 2 + (y == 0 ? 0 : 1)) * nx + x];
+                ryn = slab[((size_t)z * 2 + (y == 0 ? 1 : 0)) * nx + x];
+            }
+            if (z == 1 || z == nz - 1) {
+                const float *slab = z == 1 ? c.rp.rpz0 : c.rp.rpz_end;
+                rzs = slab[(size_t)(z == 1 ? 0 : 1) * plane + col];
+                rzn = slab[(size_t)(z == 1 ? 1 : 0) * plane + col];
+            }
+        }
         // ---- H^{n+1/2} at plane z, own cell (fdtd_calculations.cu:43-76)
         float hxn = 0.0f, hyn = 0.0f, hzn = 0.0f;
         if (in_dom) {
@@ -432,7 +457,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             }
 
             // ---- Mur faces (fdtd_calculations.cu:216-428), when fused
-            if (a.fuse_mur) {
+            if (MUR) {
                 const float dt = c.dt, me = c.me;
                 const bool fix = c.scheme == FDTD_SCHEME_CORRECTED;
                 const float pre0 = en0, pre1 = en1;  // E^{n+1} before any face value
@@ -447,8 +472,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                         auto xg = [&](int comp, int yy, int xx) { return xchg[(comp * TY + yy) * FTX + xx]; };
                         const bool zm = z >= 1 && z < nz - 1, zl = z < nz - 1;
                         if (x == 0) {
-                            const size_t b = ((size_t)z * ny + y) * 2;
-                            const float rs = c.rp.rpx0[b], rn = c.rp.rpx0[b + 1];
+                            const float rs = rxs, rn = rxn;
                             if (y < ny - 1 && zm) {
                                 en1 = mur_value(dt, c.hx, me, rs, rn, xg(1, ty, tx + 1), ea(1, r, cc + 1), ea(1, r, cc));
                                 w1 = true;
@@ -458,8 +482,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                                 w2 = true;
                             }
                         } else if (x == nx - 1) {
-                            const size_t b = ((size_t)z * ny + y) * 2;
-                            const float rs = c.rp.rpx_end[b + 1], rn = c.rp.rpx_end[b];
+                            const float rs = rxs, rn = rxn;
                             if (y < ny - 1 && zm) {
                                 // the reference reads E^n at x-1 in the first term here (:323)
                                 const float t1 = fix ? xg(1, ty, tx - 1) : ea(1, r, cc - 1);
@@ -472,8 +495,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                             }
                         }
                         if (y == 0) {
-                            const float rs = c.rp.rpy0[((size_t)z * 2 + 0) * nx + x];
-                            const float rn = c.rp.rpy0[((size_t)z * 2 + 1) * nx + x];
+                            const float rs = rys, rn = ryn;
                             if (x < nx - 1 && zm) {
                                 en0 = mur_value(dt, c.hy, me, rs, rn, xg(0, ty + 1, tx), ea(0, r + 1, cc), ea(0, r, cc));
                                 w0 = true;
@@ -483,8 +505,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                                 w2 = true;
                             }
                         } else if (y == ny - 1) {
-                            const float rs = c.rp.rpy_end[((size_t)z * 2 + 1) * nx + x];
-                            const float rn = c.rp.rpy_end[((size_t)z * 2 + 0) * nx + x];
+                            const float rs = rys, rn = ryn;
                             if (x < nx - 1 && zm) {
                                 en0 = mur_value(dt, c.hy, me, rs, rn, xg(0, ty - 1, tx), ea(0, r - 1, cc), ea(0, r, cc));
                                 w0 = true;
@@ -499,7 +520,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                 if (in_dom) {
                     const size_t pz = (size_t)y * nx + x;
                     if (z == nz - 1) {  // far z face from the plane below, kept in registers
-                        const float rs = c.rp.rpz_end[(size_t)1 * plane + pz], rn = c.rp.rpz_end[pz];
+                        const float rs = rzs, rn = rzn;
                         if (x < nx - 1 && y >= 1 && y < ny - 1) {
                             en0 = mur_value(dt, c.hz, me, rs, rn, en_prev0, e_prev_n0, ea(0, r, cc));
                             w0 = true;
@@ -510,7 +531,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                         }
                     }
                     if (z == 1) {  // near z face (plane 0), one plane late
-                        const float rs = c.rp.rpz0[pz], rn = c.rp.rpz0[(size_t)1 * plane + pz];
+                        const float rs = rzs, rn = rzn;
                         if (x < nx - 1 && y >= 1 && y < ny - 1)
                             c.e_prev[0][pz] = mur_value(dt, c.hz, me, rs, rn, pre0, ea(0, r, cc), e_prev_n0);
                         if (x >= 1 && x < nx - 1 && y < ny - 1)
@@ -534,11 +555,11 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         // refill the stage of plane k with plane k + S
         const int kn = k + S;
         if (TMA) {
-            if (tid == 0 && kn < nplanes) {
+            if (tid < 32 && kn < nplanes) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const int zn = p0 + kn;
                 issue_plane_tma<TY>(maps, stage(kn), smem_addr(&bars[kn % S]), plane_kind<TY>(zn, zc0, zc1), x0, y0,
-                                    zn);
+                                    zn, tid);
             }
         } else {
             if (kn < nplanes) {
@@ -552,13 +573,10 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         cp_async_wait<0>();
     __syncthreads();
     if (tid == 0)
-        finish_cta(c, a.fuse_mur, a.done, a.total_ctas);
+        finish_cta(c, MUR, a.done, a.total_ctas);
 }
 
 // ------------------------------------------------------------------ host side
-
-constexpr int TY_SEL = 8;
-constexpr int S_SEL = 3;
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
@@ -592,25 +610,65 @@ bool encode_map(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
-template <bool TMA>
-int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
+template <int TY>
+bool encode_all(const NativeConsts &c, FusedMaps *maps)
 {
-    using G = Geo<TY_SEL>;
-    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA>;
-    const int smem =
-        128 + S_SEL * G::STAGE + G::HN_BYTES + G::XCHG_BYTES + a.c.nclasses * (int)sizeof(DebyeCoef) + S_SEL * 8;
+    using G = Geo<TY>;
+    auto fn = encode_fn();
+    bool ok = fn != nullptr;
+    for (int k = 0; k < 3 && ok; k++) {
+        ok &= encode_map(fn, &maps->m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, G::EW, G::EH);
+        ok &= encode_map(fn, &maps->m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, G::HW, G::HH);
+        ok &= encode_map(fn, &maps->m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, FTX, TY);
+        ok &= encode_map(fn, &maps->m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, FTX, TY);
+        ok &= encode_map(fn, &maps->m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, FTX, TY);
+    }
+    return ok && encode_map(fn, &maps->m[15], c.mat, true, c.nx, c.ny, c.nz, FTX, TY);
+}
+
+template <int TY, int S, bool TMA, bool MUR>
+int launch_variant(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
+{
+    using G = Geo<TY>;
+    auto kernel = fused_step_kernel<TY, S, TMA, MUR>;
+    constexpr int XB = MUR ? G::XCHG_BYTES : 0;
+    const int smem = 128 + S * G::STAGE + G::HN_BYTES + XB + a.c.nclasses * (int)sizeof(DebyeCoef) + S * 8;
     static std::once_flag once;
     std::call_once(once, [&] {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             128 + S_SEL * G::STAGE + G::HN_BYTES + G::XCHG_BYTES +
-                                 FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) + S_SEL * 8);
+                             128 + S * G::STAGE + G::HN_BYTES + XB + FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) + S * 8);
     });
-    const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
+    const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY - 1) / TY, (a.c.nz + a.zchunk - 1) / a.zchunk);
     FusedArgs b = a;
     b.total_ctas = grid.x * grid.y * grid.z;
-    kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(b, maps);
+    kernel<<<grid, dim3(FTX, TY), smem, s>>>(b, maps);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FDTD_OK : (int)e;
+}
+
+// Kernel shape: tile height TY (8 or 16), ring depth S, Mur faces inside the
+// kernel or not.  Defaults come from measurements on the 512x512x400 phantom;
+// FDTD_FUSED_TY / FDTD_FUSED_STAGES / FDTD_FUSED_MUR override them.
+struct Shape {
+    int ty, stages;
+    bool mur;
+};
+
+int env_int(const char *name, int dflt)
+{
+    const char *v = getenv(name);
+    return v ? atoi(v) : dflt;
+}
+
+Shape fused_shape()
+{
+    Shape sh{env_int("FDTD_FUSED_TY", 8), env_int("FDTD_FUSED_STAGES", 3), env_int("FDTD_FUSED_MUR", 0) != 0};
+    if (getenv("FDTD_SEPARATE_MUR"))
+        sh.mur = false;
+    const bool known = (sh.ty == 8 && (sh.stages == 3 || sh.stages == 4)) || (sh.ty == 16 && sh.stages == 2);
+    if (!known)
+        sh.ty = 8, sh.stages = 3;
+    return sh;
 }
 
 }  // namespace
@@ -625,22 +683,8 @@ int fused_zchunk(int nz)
 
 int fused_zchunk_for(const NativeConsts &c)
 {
-    const char *env = getenv("FDTD_ZCHUNK");
-    int z = env ? atoi(env) : fused_zchunk(c.nz);
+    int z = env_int("FDTD_ZCHUNK", fused_zchunk(c.nz));
     return z < 1 ? c.nz : z;
-}
-
-// Mur faces can be computed inside the fused kernel when every face cell's
-// inner neighbour lies in the same CTA: the last x tile and the last y tile
-// hold at least two columns/rows and the first and last z chunks at least two
-// planes.  Otherwise the separate face kernel runs after it.
-bool fused_mur_ok(const NativeConsts &c)
-{
-    if (getenv("FDTD_SEPARATE_MUR"))
-        return false;
-    const int zc = fused_zchunk_for(c);
-    const int last = c.nz - ((c.nz - 1) / zc) * zc;
-    return zc >= 2 && last >= 2 && c.nx % FTX != 1 && c.ny % TY_SEL != 1;
 }
 
 bool fused_uses_tma(const NativeConsts &c)
@@ -654,32 +698,59 @@ bool fused_uses_tma(const NativeConsts &c)
     return aligned16(c.mat);
 }
 
+// The variant a launch uses.  Mur faces can be computed inside the fused
+// kernel (32 x 8 tiles, three stages) when every face cell's inner neighbour
+// lies in the same CTA: the last x tile and the last y tile hold at least two
+// columns/rows and the first and last z chunks at least two planes; otherwise
+// the separate face kernel runs after it.
+struct Decision {
+    bool tma;
+    int ty, stages;
+    bool mur;
+};
+
+Decision decide(const NativeConsts &c)
+{
+    const Shape sh = fused_shape();
+    Decision d{fused_uses_tma(c), 8, 3, false};
+    if (d.tma) {
+        d.ty = sh.ty;
+        d.stages = sh.stages;
+    }
+    const int zc = fused_zchunk_for(c);
+    const int last = c.nz - ((c.nz - 1) / zc) * zc;
+    d.mur = sh.mur && d.ty == 8 && d.stages == 3 && zc >= 2 && last >= 2 && c.nx % FTX != 1 && c.ny % d.ty != 1;
+    return d;
+}
+
+bool fused_mur_ok(const NativeConsts &c) { return decide(c).mur; }
+
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
 {
     FusedArgs a;
     a.c = c;
     a.zchunk = fused_zchunk_for(c);
-    a.fuse_mur = fused_mur_ok(c) ? 1 : 0;
     a.done = c.done;
     a.total_ctas = 0;
+    const Decision d = decide(c);
+    a.fuse_mur = d.mur ? 1 : 0;
     FusedMaps maps;
     memset(&maps, 0, sizeof maps);
-    if (fused_uses_tma(c)) {
-        auto fn = encode_fn();
-        using G = Geo<TY_SEL>;
-        bool ok = true;
-        for (int k = 0; k < 3 && ok; k++) {
-            ok &= encode_map(fn, &maps.m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, G::EW, G::EH);
-            ok &= encode_map(fn, &maps.m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, G::HW, G::HH);
-            ok &= encode_map(fn, &maps.m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
-            ok &= encode_map(fn, &maps.m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
-            ok &= encode_map(fn, &maps.m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+    if (d.tma) {
+        if (d.ty == 16) {
+            if (encode_all<16>(c, &maps))
+                return launch_variant<16, 2, true, false>(a, maps, s);
+        } else if (encode_all<8>(c, &maps)) {
+            if (d.stages == 4)
+                return launch_variant<8, 4, true, false>(a, maps, s);
+            return d.mur ? launch_variant<8, 3, true, true>(a, maps, s) : launch_variant<8, 3, true, false>(a, maps, s);
         }
-        ok &= encode_map(fn, &maps.m[15], c.mat, true, c.nx, c.ny, c.nz, FTX, TY_SEL);
-        if (ok)
-            return launch_fused_impl<true>(a, maps, s);
     }
-    return launch_fused_impl<false>(a, maps, s);
+    // generic staging (any nx, any alignment, or a tensor map that failed to
+    // encode): 32 x 8 tiles, three stages
+    if (d.mur)
+        return launch_variant<8, 3, false, true>(a, maps, s);
+    return launch_variant<8, 3, false, false>(a, maps, s);
 }
 
 int launch_step(const NativeConsts &c, cudaStream_t s)

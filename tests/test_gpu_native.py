@@ -97,3 +97,27 @@ def test_single_pass_small_z_chunks(cuda, monkeypatch, dims, chunk):
     raw = make_params(dims, consts, sources, jz)
     got = run_native(cuda, raw, specs, codes, rp, steps, mode="single")
     assert_fields_close(got, st.latest(steps))
+
+
+VARIANTS = [{"FDTD_FUSED_MUR": "1"}, {"FDTD_FUSED_TY": "16", "FDTD_FUSED_STAGES": "2"},
+            {"FDTD_FUSED_STAGES": "4"}, {"FDTD_FUSED_MUR": "0"}]
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=lambda v: ",".join(f"{k[11:]}={x}" for k, x in v.items()))
+@pytest.mark.parametrize("dims,seed", [((64, 40, 70), 12), ((48, 17, 9), 13), ((33, 26, 10), 14)])
+def test_single_pass_kernel_variants(cuda, monkeypatch, variant, dims, seed):
+    """Every tile/ring/Mur variant of the single-pass kernel against the FP32
+    oracle (TMA staging for nx % 16 == 0, cp.async otherwise)."""
+    for k, v in variant.items():
+        monkeypatch.setenv(k, v)
+    nx, ny, nz = dims
+    codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, seed, nsrc=3)
+    steps = 7
+    media = class_media(codes, specs, rp)
+    for corrected in (False, True):
+        st = po.State(nx, ny, nz, np.float32 if not corrected else np.float64)
+        po.run(po.make_cfg(dims, jz, sources=sources, consts=consts, corrected=corrected), media, st, 0, steps)
+        raw = make_params(dims, consts, sources, jz)
+        got = run_native(cuda, raw, specs, codes, rp, steps, mode="single",
+                         scheme=fg.SCHEME_CORRECTED if corrected else fg.SCHEME_REFERENCE)
+        assert_fields_close(got, st.latest(steps))
