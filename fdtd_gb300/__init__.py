@@ -37,6 +37,7 @@ FDTD_ERR_DEVICE_TIMEOUT = 10007
 MAX_SOURCES = 16
 JZ_LEN = 65536
 MAX_CLASSES = 256
+STATIC_MAX_CLASSES = 64
 SCHEME_REFERENCE = 0
 SCHEME_CORRECTED = 1
 KERNEL_SINGLE_PASS = 0
@@ -134,6 +135,7 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_step_h", _I, _V, C.POINTER(NativeFields), _V)
         _sig(L, "fdtd_step_de", _I, _V, C.POINTER(NativeFields), _I, _V)
         _sig(L, "fdtd_step", _I, _V, C.POINTER(NativeFields), _I, _V)
+        _sig(L, "fdtd_step_static", _I, PP, _P, _I, _I, C.POINTER(NativeFields), C.POINTER(_V), _I, _V)
         _sig(L, "fdtd_solver_create", _I, C.POINTER(SolverConfig), C.POINTER(_V))
         _sig(L, "fdtd_solver_destroy", _I, _V)
         _sig(L, "fdtd_solver_run", _I, _V, _I)

@@ -245,6 +245,29 @@ int fdtd_step_de(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd
  * must not alias hx..hz (H is double-buffered). */
 int fdtd_step(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd_stream_t stream);
 
+/* One single-pass step (as fdtd_step) that allocates no device memory.
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc:
+ * a process whose device memory belongs to another allocator (a framework's
+ * caching pool, a budget fixed at start-up) or code where an allocation is
+ * not allowed.  Instead of a plan it keeps the per-class Debye table, this
+ * step's source sample and an error word in a file-scope __device__ array of
+ * FDTD_STATIC_SCRATCH_BYTES bytes, which every GPU that loads the library
+ * holds until the process exits; everything else comes from the caller:
+ * p (grid, dt, dx.., sources, host jz table), specs (host, nclasses x 4,
+ * nclasses <= FDTD_STATIC_MAX_CLASSES, else FDTD_ERR_INVALID), the device
+ * fields f (hx_out..hz_out must not alias hx..hz), the six device Mur slabs
+ * rp_dev (rpx0, rpy0, rpz0, rpxEnd, rpyEnd, rpzEnd) and the step index n.
+ * The first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the array and it keeps the last call's contents (each call rewrites
+ * the table and the sample and clears the error word), so calls whose work
+ * overlaps on the GPU race.  Returns after the step has finished on the GPU:
+ * FDTD_OK, a CUDA error, or FDTD_ERR_DEVICE_TIMEOUT. */
+#define FDTD_STATIC_MAX_CLASSES 64
+#define FDTD_STATIC_SCRATCH_BYTES (FDTD_STATIC_MAX_CLASSES * 32 + 256)
+int fdtd_step_static(const FdtdParams *p, const float *specs, int nclasses, int scheme,
+                     const fdtd_native_fields *f, const float *const rp_dev[6], int n, fdtd_stream_t stream);
+
 /* ------------------------------------------------------------------------
  * Solver handle: owns the device state of one solve, runs the step loop as
  * a CUDA graph and streams snapshots through pinned buffers on a side stream.
