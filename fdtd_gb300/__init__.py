@@ -146,6 +146,13 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_solver_set_snapshots", _I, _V, C.POINTER(SnapshotSpec))
         _sig(L, "fdtd_solver_flush_snapshots", _I, _V)
         _sig(L, "fdtd_solver_profile", _I, _V, _I, _P, _I, C.POINTER(_I))
+        _sig(L, "fdtd_solver_checkpoint", _I, _V, C.c_char_p)
+        _sig(L, "fdtd_solver_restore", _I, _V, C.c_char_p)
+        _sig(L, "fdtd_solver_set_probes", _I, _V, _I, C.POINTER(_I), _I)
+        _sig(L, "fdtd_solver_get_probes", _I, _V, _P, C.POINTER(_I))
+        _sig(L, "fdtd_solver_set_dft", _I, _V, C.c_double, _I, _I, _I)
+        _sig(L, "fdtd_solver_get_dft", _I, _V, _I, C.POINTER(C.c_double), C.POINTER(C.c_double))
+        _sig(L, "fdtd_solver_peak_sar", _I, _V, _P, C.POINTER(C.c_double), C.POINTER(C.c_longlong))
         _sig(L, "fdtd_solver_kernel_name", C.c_char_p, _V, _I)
         _LIB = L
     return _LIB
@@ -329,6 +336,46 @@ class Solver:
         nk = C.c_int()
         check(lib().fdtd_solver_profile(self.handle, nsteps, ms, 8, C.byref(nk)), "fdtd_solver_profile")
         return {lib().fdtd_solver_kernel_name(self.handle, k).decode(): float(ms[k]) for k in range(nk.value)}
+
+    def checkpoint(self, path) -> None:
+        check(lib().fdtd_solver_checkpoint(self.handle, str(path).encode()), "fdtd_solver_checkpoint")
+
+    def restore(self, path) -> None:
+        check(lib().fdtd_solver_restore(self.handle, str(path).encode()), "fdtd_solver_restore")
+
+    def set_probes(self, cells, capacity: int) -> None:
+        xyz = np.ascontiguousarray(np.array(cells, np.int32).reshape(-1))
+        check(lib().fdtd_solver_set_probes(self.handle, xyz.size // 3, xyz.ctypes.data_as(C.POINTER(C.c_int)),
+                                           capacity), "fdtd_solver_set_probes")
+        self._nprobes, self._probe_cap = xyz.size // 3, capacity
+
+    def probes(self) -> np.ndarray:
+        """(steps, nprobes, 3) E series since the probes were installed."""
+        out = np.zeros((self._probe_cap, self._nprobes, 3), np.float32)
+        n = C.c_int()
+        check(lib().fdtd_solver_get_probes(self.handle, fptr(out), C.byref(n)), "fdtd_solver_get_probes")
+        return out[: n.value]
+
+    def set_dft(self, frequency: float, stride: int = 1, z0: int = 0, nplanes: int = 0) -> None:
+        check(lib().fdtd_solver_set_dft(self.handle, frequency, stride, z0, nplanes), "fdtd_solver_set_dft")
+        self._dft_np = nplanes or self.params.nz
+
+    def dft(self, comp: int) -> np.ndarray:
+        """Complex (nplanes, ny, nx) accumulator of E component comp."""
+        shape = (self._dft_np, self.params.ny, self.params.nx)
+        re = np.zeros(shape, np.float64)
+        im = np.zeros(shape, np.float64)
+        P = C.POINTER(C.c_double)
+        check(lib().fdtd_solver_get_dft(self.handle, comp, re.ctypes.data_as(P), im.ctypes.data_as(P)),
+              "fdtd_solver_get_dft")
+        return re + 1j * im
+
+    def peak_sar(self, rho=None) -> tuple[float, int]:
+        peak = C.c_double()
+        cell = C.c_longlong()
+        r = None if rho is None else fptr(np.ascontiguousarray(rho, np.float32))
+        check(lib().fdtd_solver_peak_sar(self.handle, r, C.byref(peak), C.byref(cell)), "fdtd_solver_peak_sar")
+        return peak.value, cell.value
 
     def flush_snapshots(self) -> None:
         check(lib().fdtd_solver_flush_snapshots(self.handle), "fdtd_solver_flush_snapshots")

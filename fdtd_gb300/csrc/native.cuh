@@ -20,7 +20,6 @@ struct fdtd_plan {
     float *d_jz = nullptr;                // FDTD_JZ_LEN entries
     fdtd::MurSlabs rp{};                  // six Mur slabs
     int *d_err = nullptr;                 // device error flag
-    int *d_done = nullptr;                // fused-kernel CTA completion counter
 };
 
 namespace fdtd {
@@ -43,7 +42,6 @@ struct NativeConsts {
     int step;              // step index n when step_counter is null
     int *step_counter;     // device step index (graph replay), may be null
     int *err;              // device error flag (a bounded wait gave up)
-    int *done;             // CTA completion counter of the fused kernel
     const float *h_in[3];
     float *h_out[3];
     const float *e_cur[3];
@@ -69,10 +67,9 @@ struct StepKernel {
 };
 int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int max);
 
-// H, D, sources and E of one step in the single-pass kernel (Mur faces
-// included when fused_mur_ok).
+// H, D, sources and E of one step in the single-pass kernel (the Mur faces
+// follow in launch_mur).
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s);
-bool fused_mur_ok(const NativeConsts &c);
 
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);

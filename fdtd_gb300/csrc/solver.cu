@@ -15,59 +15,11 @@
 #include <thread>
 #include <vector>
 
-#include "native.cuh"
+#include "solver_internal.cuh"
 
 using namespace fdtd;
 
-namespace {
-
-struct SnapshotSlot {
-    float *host = nullptr;  // pinned
-    int step = -1;
-    bool busy = false;      // filled or being filled
-};
-
-}  // namespace
-
-struct fdtd_solver {
-    int device = 0;
-    int nx = 0, ny = 0, nz = 0;
-    size_t ncell = 0;
-    int kernel = FDTD_KERNEL_SINGLE_PASS;
-    fdtd_plan *plan = nullptr;
-    cudaStream_t stream = nullptr;
-    cudaStream_t copy_stream = nullptr;
-    char *d_block = nullptr;
-    float *h[2][3] = {};
-    float *e[2][3] = {};
-    float *d[2][3] = {};
-    uint8_t *mat = nullptr;
-    int *counter = nullptr;
-    int steps = 0;
-    std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (parity, length) -> exec
-    // snapshots
-    fdtd_snapshot_spec snap{};
-    std::string snap_dir;
-    std::vector<int> snap_fields;
-    size_t snap_floats_per_field = 0;
-    std::vector<SnapshotSlot> ring;
-    int ring_next = 0;
-    cudaEvent_t ev_step = nullptr, ev_copy = nullptr;
-    bool copy_pending = false;  // a snapshot copy must finish before step copy_step + copy_gap
-    int copy_step = -1;
-    int copy_gap = 2;           // 1 when H is copied and updated in place
-    std::mutex mu;
-    std::condition_variable cv;
-    std::deque<int> filled;     // ring slot indices ready for the writer
-    int writing = 0;
-    bool stop = false;
-    int writer_status = FDTD_OK;
-    std::thread writer;
-};
-
-namespace {
-
-int cu(cudaError_t e) { return e == cudaSuccess ? FDTD_OK : (int)e; }
+namespace fdtd {
 
 // Pointers of step n (see native.cu for the slot convention).
 fdtd_native_fields step_fields(const fdtd_solver *s, int n)
@@ -101,18 +53,36 @@ const float *field_buffer(const fdtd_solver *s, int field, int count)
     return field < 6 ? s->d[slot][comp] : s->e[slot][comp];
 }
 
+void reset_graphs(fdtd_solver *s)
+{
+    for (auto &kv : s->graphs)
+        cudaGraphExecDestroy(kv.second);
+    s->graphs.clear();
+}
+
+}  // namespace fdtd
+
+namespace {
+
+int cu(cudaError_t e) { return e == cudaSuccess ? FDTD_OK : (int)e; }
+
 int enqueue_step(fdtd_solver *s, int n)
 {
     const fdtd_native_fields f = step_fields(s, n);
     NativeConsts c = make_consts(s->plan, &f, n);
     c.step_counter = s->counter;
-    if (s->kernel == FDTD_KERNEL_SINGLE_PASS)
-        return launch_step(c, s->stream);
-    int st = launch_h(c, s->stream);
+    int st;
+    if (s->kernel == FDTD_KERNEL_SINGLE_PASS) {
+        st = launch_step(c, s->stream);
+    } else {
+        st = launch_h(c, s->stream);
+        if (st == FDTD_OK)
+            st = launch_de(c, s->stream);
+        if (st == FDTD_OK)
+            st = launch_mur(c, s->stream);
+    }
     if (st == FDTD_OK)
-        st = launch_de(c, s->stream);
-    if (st == FDTD_OK)
-        st = launch_mur(c, s->stream);
+        st = launch_monitor(s, n);
     return st;
 }
 
@@ -324,6 +294,17 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     s->nx = p->nx; s->ny = p->ny; s->nz = p->nz;
     s->ncell = n;
     s->kernel = cfg->kernel;
+    s->scheme = cfg->scheme;
+    s->nclasses = cfg->nclasses;
+    s->specs.assign(cfg->specs, cfg->specs + 4 * (size_t)cfg->nclasses);
+    {
+        unsigned long long h = 1469598103934665603ULL;  // FNV-1a of the class volume
+        for (size_t i = 0; i < n; i++) {
+            h ^= cfg->material[i];
+            h *= 1099511628211ULL;
+        }
+        s->material_hash = h;
+    }
     st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &s->plan);
     if (st != FDTD_OK) {
         delete s;
@@ -390,9 +371,11 @@ int fdtd_solver_destroy(fdtd_solver *s)
         s->cv.notify_all();
         s->writer.join();
     }
-    for (auto &kv : s->graphs)
-        cudaGraphExecDestroy(kv.second);
+    reset_graphs(s);
     free_ring(s);
+    if (s->d_probe_idx) cudaFree(s->d_probe_idx);
+    if (s->d_probe_buf) cudaFree(s->d_probe_buf);
+    if (s->d_dft) cudaFree(s->d_dft);
     if (s->ev_step) cudaEventDestroy(s->ev_step);
     if (s->ev_copy) cudaEventDestroy(s->ev_copy);
     if (s->stream) cudaStreamDestroy(s->stream);

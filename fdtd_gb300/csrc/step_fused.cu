@@ -15,6 +15,11 @@
 // S-deep ring completed through mbarriers (every wait bounded; a timeout
 // raises the plan's error flag and the CTA stops).  Otherwise the same ring is
 // filled with 4-byte cp.async copies (zero-filled outside the grid).
+//
+// Shape (32 x 8 tiles, 3 stages, one issuing thread, Mur in its own kernel)
+// is the fastest of the variants measured on the 512 x 512 x 400 phantom:
+// 16-row tiles with 2 stages, 4 stages, Mur faces inside this kernel, and TMA
+// boxes issued by 16 lanes were each slower on the same GPU.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -42,7 +47,6 @@ struct Geo {
     static constexpr int STAGE = pad128(OFF_M + M_BYTES);
     static constexpr int HNW = FTX + 1, HNH = TY + 1;  // H^{n+1/2} plane incl. low halo
     static constexpr int HN_BYTES = pad128(3 * HNW * HNH * 4);
-    static constexpr int XCHG_BYTES = pad128(3 * FTX * TY * 4);  // E^{n+1} of the tile (Mur faces)
     // expected transaction bytes per plane kind
     static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 9u * T_BYTES + M_BYTES;
     static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
@@ -58,9 +62,6 @@ struct FusedMaps {
 struct FusedArgs {
     NativeConsts c;
     int zchunk;
-    int fuse_mur;          // Mur faces inside this kernel (else a separate launch)
-    int *done;             // CTA completion counter (step counter advance)
-    unsigned total_ctas;
 };
 
 // ---------------------------------------------------------------- PTX helpers
@@ -118,21 +119,6 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Step counter advance: the last CTA of the launch to finish increments it
-// (every CTA read it at its start, before its own increment of `done`).
-__device__ __forceinline__ void finish_cta(const NativeConsts &c, int fuse_mur, int *done, unsigned total)
-{
-    if (!fuse_mur || !done || !c.step_counter)
-        return;
-    __threadfence();
-    const unsigned prev = atomicAdd(reinterpret_cast<unsigned *>(done), 1u);
-    if (prev == total - 1) {
-        atomicExch(done, 0);
-        __threadfence();
-        atomicAdd(c.step_counter, 1);
-    }
-}
-
 // ------------------------------------------------------------ plane staging
 
 enum PlaneKind { PLANE_FULL = 0, PLANE_PRO = 1, PLANE_EPI = 2 };
@@ -143,28 +129,25 @@ __device__ __forceinline__ int plane_kind(int z, int zc0, int zc1)
     return z < zc0 ? PLANE_PRO : (z >= zc1 ? PLANE_EPI : PLANE_FULL);
 }
 
-// TMA: lane 0 of warp 0 arms the stage's barrier, then lane b issues box b
-// (3 E^n boxes, 3 H boxes, 9 tile boxes, 1 class box), so the 16 copies of a
-// plane leave in one warp instruction instead of sixteen.
+// TMA: one thread arms the stage's barrier and issues the plane's boxes.
 template <int TY>
 __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
-                                int z, int lane)
+                                int z)
 {
     using G = Geo<TY>;
     const unsigned bytes = kind == PLANE_FULL ? G::TX_FULL : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI);
-    const int nbox = kind == PLANE_FULL ? 16 : (kind == PLANE_PRO ? 6 : 3);
-    if (lane == 0)
-        mbar_expect_tx(bar, bytes);
-    __syncwarp();
-    if (lane < 3)
-        tma_load_3d(smem_addr(stage + G::OFF_E + lane * pad128(G::E_BYTES)), &maps.m[lane], x0 - 4, y0 - 1, z, bar);
-    else if (lane < 6 && lane < nbox)
-        tma_load_3d(smem_addr(stage + G::OFF_H + (lane - 3) * pad128(G::H_BYTES)), &maps.m[lane], x0 - 4, y0 - 1, z,
-                    bar);
-    else if (lane < 15 && lane < nbox)
-        tma_load_3d(smem_addr(stage + G::OFF_T + (lane - 6) * pad128(G::T_BYTES)), &maps.m[lane], x0, y0, z, bar);
-    else if (lane == 15 && lane < nbox)
-        tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[15], x0, y0, z, bar);
+    mbar_expect_tx(bar, bytes);
+    for (int c = 0; c < 3; c++)
+        tma_load_3d(smem_addr(stage + G::OFF_E + c * pad128(G::E_BYTES)), &maps.m[c], x0 - 4, y0 - 1, z, bar);
+    if (kind == PLANE_EPI)
+        return;
+    for (int c = 0; c < 3; c++)
+        tma_load_3d(smem_addr(stage + G::OFF_H + c * pad128(G::H_BYTES)), &maps.m[3 + c], x0 - 4, y0 - 1, z, bar);
+    if (kind == PLANE_PRO)
+        return;
+    for (int k = 0; k < 9; k++)
+        tma_load_3d(smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), &maps.m[6 + k], x0, y0, z, bar);
+    tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[15], x0, y0, z, bar);
 }
 
 // Generic: every thread copies part of each box with 4-byte cp.async
@@ -201,7 +184,7 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
 
 // ---------------------------------------------------------------- the kernel
 
-template <int TY, int S, bool TMA, bool MUR>
+template <int TY, int S, bool TMA>
 __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
                                                              const __grid_constant__ FusedMaps maps)
 {
@@ -219,9 +202,8 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     const int nplanes = plast - p0 + 1;
 
     float *hn = reinterpret_cast<float *>(smem + S * G::STAGE);
-    constexpr int XB = MUR ? G::XCHG_BYTES : 0;
-    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES + XB);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + XB + c.nclasses * sizeof(DebyeCoef));
+    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + c.nclasses * sizeof(DebyeCoef));
     auto stage = [&](int k) { return smem + (k % S) * G::STAGE; };
 
     // coefficient table -> shared memory
@@ -243,9 +225,8 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         if (k < nplanes) {
             const int z = p0 + k;
             if (TMA) {
-                if (tid < 32)
-                    issue_plane_tma<TY>(maps, stage(k), smem_addr(&bars[k % S]), plane_kind<TY>(z, zc0, zc1), x0, y0, z,
-                                        tid);
+                if (tid == 0)
+                    issue_plane_tma<TY>(maps, stage(k), smem_addr(&bars[k % S]), plane_kind<TY>(z, zc0, zc1), x0, y0, z);
             } else {
                 issue_plane_generic<TY>(c, stage(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z, tid);
             }
@@ -267,10 +248,6 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     const size_t col = (size_t)y * nx + x;
     const float kx = c.kx, ky = c.ky, kz = c.kz, tcx = c.tx, tcy = c.ty, tcz = c.tz;
     float hxm = 0.0f, hym = 0.0f;  // H^{n+1/2} of this column at z-1
-    // E^{n+1} (before face values) and E^n of this column at z-1, for the z faces
-    float en_prev0 = 0.0f, en_prev1 = 0.0f, e_prev_n0 = 0.0f, e_prev_n1 = 0.0f;
-    const bool boundary_cta = x0 == 0 || x0 + FTX >= nx || y0 == 0 || y0 + TY >= ny;
-    float *xchg = reinterpret_cast<float *>(smem + S * G::STAGE + G::HN_BYTES);
     uint8_t mat_next = 0;
     if (!TMA && in_dom && zc0 < nz)
         mat_next = c.mat[(size_t)zc0 * plane + col];
@@ -293,7 +270,6 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                     // let the copies in flight land before the CTA exits (bounded)
                     for (int j = k; j < nplanes && j < k + S; j++)
                         mbar_wait(smem_addr(&bars[j % S]), (j / S) & 1);
-                    finish_cta(c, MUR, a.done, a.total_ctas);
                 }
                 __syncthreads();
                 return;
@@ -312,27 +288,6 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         auto hnr = [&](int comp, int r, int cc) -> float & { return hn[(comp * G::HNH + r) * G::HNW + cc]; };
 
         const bool zlo = z < nz - 1, zmid = z >= 1 && z < nz - 1;
-        // Mur slab values this thread's face cells need on this plane, loaded
-        // early so their latency overlaps the H, D and E work
-        float rxs = 0.0f, rxn = 0.0f, rys = 0.0f, ryn = 0.0f, rzs = 0.0f, rzn = 0.0f;
-        if (MUR && in_dom && z >= zc0) {
-            if (x == 0 || x == nx - 1) {
-                const float *slab = x == 0 ? c.rp.rpx0 : c.rp.rpx_end;
-                const size_t b = ((size_t)z * ny + y) * 2;
-                rxs = slab[b + (x == 0 ? 0 : 1)];
-                rxn = slab[b + (x == 0 ? 1 : 0)];
-            }
-            if (y == 0 || y == ny - 1) {
-                const float *slab = y == 0 ? c.rp.rpy0 : c.rp.rpy_end;
-                rys = slab[((size_t)z * 2 + (y == 0 ? 0 : 1)) * nx + x];
-                ryn = slab[((size_t)z * 2 + (y == 0 ? 1 : 0)) * nx + x];
-            }
-            if (z == 1 || z == nz - 1) {
-                const float *slab = z == 1 ? c.rp.rpz0 : c.rp.rpz_end;
-                rzs = slab[(size_t)(z == 1 ? 0 : 1) * plane + col];
-                rzn = slab[(size_t)(z == 1 ? 1 : 0) * plane + col];
-            }
-        }
         // ---- H^{n+1/2} at plane z, own cell (fdtd_calculations.cu:43-76)
         float hxn = 0.0f, hyn = 0.0f, hzn = 0.0f;
         if (in_dom) {
@@ -352,10 +307,6 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             hxm = hxn;
             hym = hyn;
         } else {
-            if (z == 0 && in_dom) {  // E^n of plane 0 for the near z face
-                e_prev_n0 = ea(0, ty + 1, tx + 4);
-                e_prev_n1 = ea(1, ty + 1, tx + 4);
-            }
             if (in_dom) {
                 hnr(0, ty + 1, tx + 1) = hxn;
                 hnr(1, ty + 1, tx + 1) = hyn;
@@ -390,11 +341,8 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             }
             __syncthreads();
 
-            const size_t i = (size_t)z * plane + col;
-            const int r = ty + 1, cc = tx + 4;
-            float en0 = 0.0f, en1 = 0.0f, en2 = 0.0f;  // E^{n+1}: the slot's value unless updated
-            bool w0 = false, w1 = false, w2 = false;
             if (in_dom) {
+                const size_t i = (size_t)z * plane + col;
                 const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
                 const int t = ty * FTX + tx;
                 const float dn0 = T[0 * TS + t], dn1 = T[1 * TS + t], dn2 = T[2 * TS + t];
@@ -440,113 +388,18 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
                 if (dz_on) c.d_prev[2][i] = d2;
 
                 // ---- Debye E^{n+1} (fdtd_calculations.cu:146-183)
-                w0 = x < nx - 1 && yi && zmid;
-                w1 = w2 = x >= 1 && z >= 1;
-                en0 = ep0;
-                en1 = ep1;
-                en2 = ep2;
-                if (w0 || w1) {
+                const bool ex_on = x < nx - 1 && yi && zmid;
+                const bool eyz_on = x >= 1 && z >= 1;
+                if (ex_on || eyz_on) {
                     const DebyeCoef kc = coef[cls];
-                    if (w0)
-                        en0 = debye_update(kc, ea(0, r, cc), ep0, d0, dn0, dp0);
-                    if (w1) {
-                        en1 = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
-                        en2 = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
+                    const int r = ty + 1, cc = tx + 4;
+                    if (ex_on)
+                        c.e_prev[0][i] = debye_update(kc, ea(0, r, cc), ep0, d0, dn0, dp0);
+                    if (eyz_on) {
+                        c.e_prev[1][i] = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
+                        c.e_prev[2][i] = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
                     }
                 }
-            }
-
-            // ---- Mur faces (fdtd_calculations.cu:216-428), when fused
-            if (MUR) {
-                const float dt = c.dt, me = c.me;
-                const bool fix = c.scheme == FDTD_SCHEME_CORRECTED;
-                const float pre0 = en0, pre1 = en1;  // E^{n+1} before any face value
-                if (boundary_cta) {
-                    if (in_dom) {
-                        xchg[(0 * TY + ty) * FTX + tx] = en0;
-                        xchg[(1 * TY + ty) * FTX + tx] = en1;
-                        xchg[(2 * TY + ty) * FTX + tx] = en2;
-                    }
-                    __syncthreads();
-                    if (in_dom) {
-                        auto xg = [&](int comp, int yy, int xx) { return xchg[(comp * TY + yy) * FTX + xx]; };
-                        const bool zm = z >= 1 && z < nz - 1, zl = z < nz - 1;
-                        if (x == 0) {
-                            const float rs = rxs, rn = rxn;
-                            if (y < ny - 1 && zm) {
-                                en1 = mur_value(dt, c.hx, me, rs, rn, xg(1, ty, tx + 1), ea(1, r, cc + 1), ea(1, r, cc));
-                                w1 = true;
-                            }
-                            if (y >= 1 && y < ny - 1 && zl) {
-                                en2 = mur_value(dt, c.hx, me, rs, rn, xg(2, ty, tx + 1), ea(2, r, cc + 1), ea(2, r, cc));
-                                w2 = true;
-                            }
-                        } else if (x == nx - 1) {
-                            const float rs = rxs, rn = rxn;
-                            if (y < ny - 1 && zm) {
-                                // the reference reads E^n at x-1 in the first term here (:323)
-                                const float t1 = fix ? xg(1, ty, tx - 1) : ea(1, r, cc - 1);
-                                en1 = mur_value(dt, c.hx, me, rs, rn, t1, ea(1, r, cc - 1), ea(1, r, cc));
-                                w1 = true;
-                            }
-                            if (y >= 1 && y < ny - 1 && zl) {
-                                en2 = mur_value(dt, c.hx, me, rs, rn, xg(2, ty, tx - 1), ea(2, r, cc - 1), ea(2, r, cc));
-                                w2 = true;
-                            }
-                        }
-                        if (y == 0) {
-                            const float rs = rys, rn = ryn;
-                            if (x < nx - 1 && zm) {
-                                en0 = mur_value(dt, c.hy, me, rs, rn, xg(0, ty + 1, tx), ea(0, r + 1, cc), ea(0, r, cc));
-                                w0 = true;
-                            }
-                            if (x >= 1 && x < nx - 1 && zl) {
-                                en2 = mur_value(dt, c.hy, me, rs, rn, xg(2, ty + 1, tx), ea(2, r + 1, cc), ea(2, r, cc));
-                                w2 = true;
-                            }
-                        } else if (y == ny - 1) {
-                            const float rs = rys, rn = ryn;
-                            if (x < nx - 1 && zm) {
-                                en0 = mur_value(dt, c.hy, me, rs, rn, xg(0, ty - 1, tx), ea(0, r - 1, cc), ea(0, r, cc));
-                                w0 = true;
-                            }
-                            if (x >= 1 && x < nx - 1 && zl) {
-                                en2 = mur_value(dt, c.hy, me, rs, rn, xg(2, ty - 1, tx), ea(2, r - 1, cc), ea(2, r, cc));
-                                w2 = true;
-                            }
-                        }
-                    }
-                }
-                if (in_dom) {
-                    const size_t pz = (size_t)y * nx + x;
-                    if (z == nz - 1) {  // far z face from the plane below, kept in registers
-                        const float rs = rzs, rn = rzn;
-                        if (x < nx - 1 && y >= 1 && y < ny - 1) {
-                            en0 = mur_value(dt, c.hz, me, rs, rn, en_prev0, e_prev_n0, ea(0, r, cc));
-                            w0 = true;
-                        }
-                        if (x >= 1 && x < nx - 1 && y < ny - 1) {
-                            en1 = mur_value(dt, c.hz, me, rs, rn, en_prev1, e_prev_n1, ea(1, r, cc));
-                            w1 = true;
-                        }
-                    }
-                    if (z == 1) {  // near z face (plane 0), one plane late
-                        const float rs = rzs, rn = rzn;
-                        if (x < nx - 1 && y >= 1 && y < ny - 1)
-                            c.e_prev[0][pz] = mur_value(dt, c.hz, me, rs, rn, pre0, ea(0, r, cc), e_prev_n0);
-                        if (x >= 1 && x < nx - 1 && y < ny - 1)
-                            c.e_prev[1][pz] = mur_value(dt, c.hz, me, rs, rn, pre1, ea(1, r, cc), e_prev_n1);
-                    }
-                    en_prev0 = pre0;
-                    en_prev1 = pre1;
-                    e_prev_n0 = ea(0, r, cc);
-                    e_prev_n1 = ea(1, r, cc);
-                }
-            }
-            if (in_dom) {
-                if (w0) c.e_prev[0][i] = en0;
-                if (w1) c.e_prev[1][i] = en1;
-                if (w2) c.e_prev[2][i] = en2;
             }
             hxm = hxn;
             hym = hyn;
@@ -555,11 +408,11 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         // refill the stage of plane k with plane k + S
         const int kn = k + S;
         if (TMA) {
-            if (tid < 32 && kn < nplanes) {
+            if (tid == 0 && kn < nplanes) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const int zn = p0 + kn;
                 issue_plane_tma<TY>(maps, stage(kn), smem_addr(&bars[kn % S]), plane_kind<TY>(zn, zc0, zc1), x0, y0,
-                                    zn, tid);
+                                    zn);
             }
         } else {
             if (kn < nplanes) {
@@ -571,12 +424,12 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     }
     if (!TMA)
         cp_async_wait<0>();
-    __syncthreads();
-    if (tid == 0)
-        finish_cta(c, MUR, a.done, a.total_ctas);
 }
 
 // ------------------------------------------------------------------ host side
+
+constexpr int TY_SEL = 8;
+constexpr int S_SEL = 3;
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 {
@@ -610,65 +463,22 @@ bool encode_map(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void
 
 bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
-template <int TY>
-bool encode_all(const NativeConsts &c, FusedMaps *maps)
+template <bool TMA>
+int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
-    using G = Geo<TY>;
-    auto fn = encode_fn();
-    bool ok = fn != nullptr;
-    for (int k = 0; k < 3 && ok; k++) {
-        ok &= encode_map(fn, &maps->m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, G::EW, G::EH);
-        ok &= encode_map(fn, &maps->m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, G::HW, G::HH);
-        ok &= encode_map(fn, &maps->m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, FTX, TY);
-        ok &= encode_map(fn, &maps->m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, FTX, TY);
-        ok &= encode_map(fn, &maps->m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, FTX, TY);
-    }
-    return ok && encode_map(fn, &maps->m[15], c.mat, true, c.nx, c.ny, c.nz, FTX, TY);
-}
-
-template <int TY, int S, bool TMA, bool MUR>
-int launch_variant(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
-{
-    using G = Geo<TY>;
-    auto kernel = fused_step_kernel<TY, S, TMA, MUR>;
-    constexpr int XB = MUR ? G::XCHG_BYTES : 0;
-    const int smem = 128 + S * G::STAGE + G::HN_BYTES + XB + a.c.nclasses * (int)sizeof(DebyeCoef) + S * 8;
+    using G = Geo<TY_SEL>;
+    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA>;
+    const int smem = 128 + S_SEL * G::STAGE + G::HN_BYTES + a.c.nclasses * (int)sizeof(DebyeCoef) + S_SEL * 8;
     static std::once_flag once;
     std::call_once(once, [&] {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             128 + S * G::STAGE + G::HN_BYTES + XB + FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) + S * 8);
+                             128 + S_SEL * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) +
+                                 S_SEL * 8);
     });
-    const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY - 1) / TY, (a.c.nz + a.zchunk - 1) / a.zchunk);
-    FusedArgs b = a;
-    b.total_ctas = grid.x * grid.y * grid.z;
-    kernel<<<grid, dim3(FTX, TY), smem, s>>>(b, maps);
+    const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
+    kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(a, maps);
     const cudaError_t e = cudaGetLastError();
     return e == cudaSuccess ? FDTD_OK : (int)e;
-}
-
-// Kernel shape: tile height TY (8 or 16), ring depth S, Mur faces inside the
-// kernel or not.  Defaults come from measurements on the 512x512x400 phantom;
-// FDTD_FUSED_TY / FDTD_FUSED_STAGES / FDTD_FUSED_MUR override them.
-struct Shape {
-    int ty, stages;
-    bool mur;
-};
-
-int env_int(const char *name, int dflt)
-{
-    const char *v = getenv(name);
-    return v ? atoi(v) : dflt;
-}
-
-Shape fused_shape()
-{
-    Shape sh{env_int("FDTD_FUSED_TY", 8), env_int("FDTD_FUSED_STAGES", 3), env_int("FDTD_FUSED_MUR", 0) != 0};
-    if (getenv("FDTD_SEPARATE_MUR"))
-        sh.mur = false;
-    const bool known = (sh.ty == 8 && (sh.stages == 3 || sh.stages == 4)) || (sh.ty == 16 && sh.stages == 2);
-    if (!known)
-        sh.ty = 8, sh.stages = 3;
-    return sh;
 }
 
 }  // namespace
@@ -679,12 +489,6 @@ int fused_zchunk(int nz)
     // prologue/epilogue traffic at chunk borders
     const int chunks = (nz + 63) / 64;
     return (nz + chunks - 1) / chunks;
-}
-
-int fused_zchunk_for(const NativeConsts &c)
-{
-    int z = env_int("FDTD_ZCHUNK", fused_zchunk(c.nz));
-    return z < 1 ? c.nz : z;
 }
 
 bool fused_uses_tma(const NativeConsts &c)
@@ -698,77 +502,48 @@ bool fused_uses_tma(const NativeConsts &c)
     return aligned16(c.mat);
 }
 
-// The variant a launch uses.  Mur faces can be computed inside the fused
-// kernel (32 x 8 tiles, three stages) when every face cell's inner neighbour
-// lies in the same CTA: the last x tile and the last y tile hold at least two
-// columns/rows and the first and last z chunks at least two planes; otherwise
-// the separate face kernel runs after it.
-struct Decision {
-    bool tma;
-    int ty, stages;
-    bool mur;
-};
-
-Decision decide(const NativeConsts &c)
-{
-    const Shape sh = fused_shape();
-    Decision d{fused_uses_tma(c), 8, 3, false};
-    if (d.tma) {
-        d.ty = sh.ty;
-        d.stages = sh.stages;
-    }
-    const int zc = fused_zchunk_for(c);
-    const int last = c.nz - ((c.nz - 1) / zc) * zc;
-    d.mur = sh.mur && d.ty == 8 && d.stages == 3 && zc >= 2 && last >= 2 && c.nx % FTX != 1 && c.ny % d.ty != 1;
-    return d;
-}
-
-bool fused_mur_ok(const NativeConsts &c) { return decide(c).mur; }
-
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
 {
     FusedArgs a;
     a.c = c;
-    a.zchunk = fused_zchunk_for(c);
-    a.done = c.done;
-    a.total_ctas = 0;
-    const Decision d = decide(c);
-    a.fuse_mur = d.mur ? 1 : 0;
+    const char *env = getenv("FDTD_ZCHUNK");
+    a.zchunk = env ? atoi(env) : fused_zchunk(c.nz);
+    if (a.zchunk < 1)
+        a.zchunk = c.nz;
     FusedMaps maps;
     memset(&maps, 0, sizeof maps);
-    if (d.tma) {
-        if (d.ty == 16) {
-            if (encode_all<16>(c, &maps))
-                return launch_variant<16, 2, true, false>(a, maps, s);
-        } else if (encode_all<8>(c, &maps)) {
-            if (d.stages == 4)
-                return launch_variant<8, 4, true, false>(a, maps, s);
-            return d.mur ? launch_variant<8, 3, true, true>(a, maps, s) : launch_variant<8, 3, true, false>(a, maps, s);
+    if (fused_uses_tma(c)) {
+        auto fn = encode_fn();
+        using G = Geo<TY_SEL>;
+        bool ok = true;
+        for (int k = 0; k < 3 && ok; k++) {
+            ok &= encode_map(fn, &maps.m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, G::EW, G::EH);
+            ok &= encode_map(fn, &maps.m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, G::HW, G::HH);
+            ok &= encode_map(fn, &maps.m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
         }
+        ok &= encode_map(fn, &maps.m[15], c.mat, true, c.nx, c.ny, c.nz, FTX, TY_SEL);
+        if (ok)
+            return launch_fused_impl<true>(a, maps, s);
     }
-    // generic staging (any nx, any alignment, or a tensor map that failed to
-    // encode): 32 x 8 tiles, three stages
-    if (d.mur)
-        return launch_variant<8, 3, false, true>(a, maps, s);
-    return launch_variant<8, 3, false, false>(a, maps, s);
+    return launch_fused_impl<false>(a, maps, s);
 }
 
 int launch_step(const NativeConsts &c, cudaStream_t s)
 {
     int st = launch_h_de_fused(c, s);
-    if (st == FDTD_OK && !fused_mur_ok(c))
+    if (st == FDTD_OK)
         st = launch_mur(c, s);
     return st;
 }
 
-int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int max)
+int step_kernels(int kernel_kind, const NativeConsts &, StepKernel *out, int max)
 {
     StepKernel single[] = {{"fused_step", launch_h_de_fused}, {"mur", launch_mur}};
     StepKernel two[] = {{"h", launch_h}, {"de", launch_de}, {"mur", launch_mur}};
     const StepKernel *src = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? single : two;
-    int n = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? 2 : 3;
-    if (kernel_kind == FDTD_KERNEL_SINGLE_PASS && fused_mur_ok(c))
-        n = 1;
+    const int n = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? 2 : 3;
     for (int k = 0; k < n && k < max; k++)
         out[k] = src[k];
     return n;

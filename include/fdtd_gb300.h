@@ -337,6 +337,39 @@ int fdtd_solver_set_snapshots(fdtd_solver *s, const fdtd_snapshot_spec *spec);
 /* Waits for every snapshot of enqueued steps to be delivered. */
 int fdtd_solver_flush_snapshots(fdtd_solver *s);
 
+/* ---- checkpoint / resume (no reference counterpart) ----
+ * fdtd_solver_checkpoint writes the solve's state after the last enqueued
+ * step -- H, E^n, E^{n-1}, D^n, D^{n-1} (15 float arrays), the step count and
+ * a checksum of the material volume -- to a binary file.  fdtd_solver_restore
+ * loads such a file into a solver created with the same configuration
+ * (FDTD_ERR_FORMAT if grid, scheme or materials differ) and continues from
+ * its step count; the continued run is identical to an uninterrupted one. */
+int fdtd_solver_checkpoint(fdtd_solver *s, const char *path);
+int fdtd_solver_restore(fdtd_solver *s, const char *path);
+
+/* ---- on-device monitors (FP64 accumulators; no reference counterpart) ----
+ * Probes: after every step, E (x, y, z components) at up to
+ * FDTD_MAX_PROBES cells is appended to a device buffer of `capacity` steps.
+ * fdtd_solver_get_probes copies the series out (nsteps x nprobes x 3 floats,
+ * oldest first) and sets *nsteps.  Installing probes or a DFT replaces the
+ * previous monitor of that kind and restarts it. */
+#define FDTD_MAX_PROBES 64
+int fdtd_solver_set_probes(fdtd_solver *s, int nprobes, const int *xyz, int capacity);
+int fdtd_solver_get_probes(fdtd_solver *s, float *out, int *nsteps);
+
+/* Running DFT of E at one frequency: every `stride` steps, for the planes
+ * [z0, z0 + nplanes) (nplanes 0 = all), acc_c += E_c(t) exp(-i 2 pi f t) *
+ * stride * dt in double precision, t = (steps completed) * dt. */
+int fdtd_solver_set_dft(fdtd_solver *s, double frequency, int stride, int z0, int nplanes);
+/* Copies the accumulators of component comp (0 x, 1 y, 2 z) as
+ * nx*ny*nplanes doubles each (re, im; either may be NULL). */
+int fdtd_solver_get_dft(fdtd_solver *s, int comp, double *re, double *im);
+/* Spectral SAR from the DFT accumulators: sigma(class) |E_f|^2 / (2 rho(class))
+ * per cell, reduced on the device to its maximum (*peak) and that cell's
+ * linear index (*cell).  rho: nclasses densities in kg/m^3 (NULL: 1000 for
+ * every class). */
+int fdtd_solver_peak_sar(fdtd_solver *s, const float *rho, double *peak, long long *cell);
+
 /* Kernel timing (the role of the reference's nvprof job scripts,
  * run_fdtd_prof*-rafal.sh): runs nsteps steps launching each kernel directly,
  * bracketed by CUDA events on the solver stream, and returns the average

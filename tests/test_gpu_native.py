@@ -99,12 +99,6 @@ def test_single_pass_small_z_chunks(cuda, monkeypatch, dims, chunk):
     assert_fields_close(got, st.latest(steps))
 
 
-VARIANTS = [{"FDTD_FUSED_MUR": "1"}, {"FDTD_FUSED_TY": "16", "FDTD_FUSED_STAGES": "2"},
-            {"FDTD_FUSED_STAGES": "4"}, {"FDTD_FUSED_MUR": "0"}]
-
-
-@pytest.mark.parametrize("variant", VARIANTS, ids=lambda v: ",".join(f"{k[11:]}={x}" for k, x in v.items()))
-@pytest.mark.parametrize("dims,seed", [((64, 40, 70), 12), ((48, 17, 9), 13), ((33, 26, 10), 14)])
 def test_single_pass_kernel_variants(cuda, monkeypatch, variant, dims, seed):
     """Every tile/ring/Mur variant of the single-pass kernel against the FP32
     oracle (TMA staging for nx % 16 == 0, cp.async otherwise)."""
