@@ -154,6 +154,18 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_solver_get_dft", _I, _V, _I, C.POINTER(C.c_double), C.POINTER(C.c_double))
         _sig(L, "fdtd_solver_peak_sar", _I, _V, _P, C.POINTER(C.c_double), C.POINTER(C.c_longlong))
         _sig(L, "fdtd_solver_kernel_name", C.c_char_p, _V, _I)
+        _sig(L, "fdtd_batch_create", _I, _I, C.POINTER(_V))
+        _sig(L, "fdtd_batch_destroy", _I, _V)
+        _sig(L, "fdtd_batch_solve_bytes", C.c_size_t, _I, _I, _I)
+        _sig(L, "fdtd_batch_add", _I, _V, C.POINTER(SolverConfig), _I, C.POINTER(_I))
+        _sig(L, "fdtd_batch_remove", _I, _V, _I)
+        _sig(L, "fdtd_batch_run", _I, _V, _I)
+        _sig(L, "fdtd_batch_synchronize", _I, _V)
+        _sig(L, "fdtd_batch_steps", _I, _V, _I)
+        _sig(L, "fdtd_batch_get_field", _I, _V, _I, _I, _I, _I, _P)
+        _sig(L, "fdtd_batch_bytes", C.c_size_t, _V)
+        _sig(L, "fdtd_batch_size", _I, _V)
+        _sig(L, "fdtd_batch_stream", _V, _V)
         _LIB = L
     return _LIB
 
@@ -390,6 +402,81 @@ class Solver:
 
     def __exit__(self, *exc):
         self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------- batch
+
+class Batch:
+    """Many independent solves advanced together (fdtd_batch_*)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        check(lib().fdtd_batch_create(device, C.byref(h)), "fdtd_batch_create")
+        self.handle = h
+        self._keep = {}
+
+    @staticmethod
+    def solve_bytes(nx: int, ny: int, nz: int) -> int:
+        return lib().fdtd_batch_solve_bytes(nx, ny, nz)
+
+    def add(self, p: Params, material: np.ndarray, specs: np.ndarray, steps: int,
+            scheme: int = SCHEME_REFERENCE, nclasses: int | None = None) -> int:
+        material = np.ascontiguousarray(material, np.uint8)
+        specs = np.ascontiguousarray(specs, np.float32).reshape(-1, 4)
+        if nclasses is None:
+            nclasses = int(material.max()) + 1
+        specs = np.ascontiguousarray(specs[:nclasses])
+        cfg = SolverConfig(params=C.pointer(p.raw), material=material.ctypes.data_as(C.POINTER(C.c_uint8)),
+                           specs=fptr(specs), nclasses=nclasses, scheme=scheme, kernel=0, device=0)
+        sid = C.c_int()
+        check(lib().fdtd_batch_add(self.handle, C.byref(cfg), steps, C.byref(sid)), "fdtd_batch_add")
+        self._keep[sid.value] = (p, (p.raw.nz, p.raw.ny, p.raw.nx))
+        return sid.value
+
+    def remove(self, sid: int) -> None:
+        check(lib().fdtd_batch_remove(self.handle, sid), "fdtd_batch_remove")
+        self._keep.pop(sid, None)
+
+    def run(self, nsteps: int) -> None:
+        check(lib().fdtd_batch_run(self.handle, nsteps), "fdtd_batch_run")
+
+    def synchronize(self) -> None:
+        check(lib().fdtd_batch_synchronize(self.handle), "fdtd_batch_synchronize")
+
+    def steps(self, sid: int) -> int:
+        return lib().fdtd_batch_steps(self.handle, sid)
+
+    def field(self, sid: int, name: str, z0: int = 0, nplanes: int = 0) -> np.ndarray:
+        nz, ny, nx = self._keep[sid][1]
+        out = np.empty((nplanes or nz, ny, nx), np.float32)
+        check(lib().fdtd_batch_get_field(self.handle, sid, FIELD_ID[name], z0, nplanes, fptr(out)),
+              "fdtd_batch_get_field")
+        return out
+
+    def fields(self, sid: int) -> dict[str, np.ndarray]:
+        return {n: self.field(sid, n) for n in FIELDS}
+
+    @property
+    def bytes(self) -> int:
+        return lib().fdtd_batch_bytes(self.handle)
+
+    @property
+    def stream(self) -> int:
+        return lib().fdtd_batch_stream(self.handle) or 0
+
+    def __len__(self) -> int:
+        return lib().fdtd_batch_size(self.handle)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            lib().fdtd_batch_destroy(self.handle)
+            self.handle = None
 
     def __del__(self):
         try:

@@ -1,0 +1,421 @@
+// batch.cu -- many independent solves of uneven sizes advanced together.
+//
+// Each solve keeps its own resident state (H x2, E x2, D x2, classes) with
+// rows padded to a multiple of 16 cells, so every solve gets TMA staging, and
+// its own plan (class table, source table, Mur slabs) and step counter.  A
+// batched step is three launches: one persistent kernel over the work units
+// (column tile x z chunk) of all solves, one Mur launch over all solves' face
+// cells, and a one-block kernel that advances the step counters.  Step n of a
+// solve uses its counter's parity to pick pointers and tensor maps, so one
+// captured graph serves every step; a solve stops once it reaches its target
+// step count.  Adding or removing a solve rebuilds the descriptors and the
+// graph.  No reference counterpart (the reference runs one grid).
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "native.cuh"
+
+using namespace fdtd;
+
+namespace {
+
+int cu(cudaError_t e) { return e == cudaSuccess ? FDTD_OK : (int)e; }
+
+struct BatchSolve {
+    int id = 0;
+    int nx = 0, ny = 0, nz = 0, pitch = 0;
+    size_t ncell = 0;  // pitch * ny * nz
+    size_t bytes = 0;
+    int steps_target = 0;
+    fdtd_plan *plan = nullptr;
+    char *d_block = nullptr;
+    float *h[2][3] = {};
+    float *e[2][3] = {};
+    float *d[2][3] = {};
+    uint8_t *mat = nullptr;
+    int *counter = nullptr;
+};
+
+size_t padded_pitch(int nx) { return ((size_t)nx + 15) & ~size_t(15); }
+
+size_t state_bytes(int nx, int ny, int nz)
+{
+    const size_t ncell = padded_pitch(nx) * ny * nz;
+    const size_t f = (ncell * sizeof(float) + 255) & ~size_t(255);
+    return 18 * f + ((ncell + 255) & ~size_t(255)) + 256;
+}
+
+}  // namespace
+
+struct fdtd_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<BatchSolve *> solves;
+    int next_id = 1;
+    bool dirty = true;
+    BatchDesc *d_descs = nullptr;
+    size_t descs_cap = 0;
+    BatchMurBlock *d_mur = nullptr;
+    size_t mur_cap = 0;
+    int *d_work = nullptr;
+    BatchLaunch launch{};
+    std::map<int, cudaGraphExec_t> graphs;  // steps per graph -> exec
+    size_t bytes = 0;
+};
+
+namespace {
+
+void free_solve(BatchSolve *v)
+{
+    if (!v)
+        return;
+    cudaFree(v->d_block);
+    fdtd_plan_destroy(v->plan);
+    delete v;
+}
+
+void drop_graphs(fdtd_batch *b)
+{
+    for (auto &kv : b->graphs)
+        cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
+}
+
+NativeConsts solve_consts(const BatchSolve *v, int parity)
+{
+    fdtd_native_fields f{};
+    const int cur = (parity + 1) & 1, prv = parity & 1;
+    for (int k = 0; k < 3; k++) {
+        (&f.hx)[k] = v->h[parity][k];
+        (&f.hx_out)[k] = v->h[(parity + 1) & 1][k];
+        (&f.ex)[k] = v->e[cur][k];
+        (&f.ex_prev)[k] = v->e[prv][k];
+        (&f.dx)[k] = v->d[cur][k];
+        (&f.dx_prev)[k] = v->d[prv][k];
+    }
+    f.material = v->mat;
+    NativeConsts c = make_consts(v->plan, &f, 0);
+    c.pitch = v->pitch;
+    c.step_counter = v->counter;
+    return c;
+}
+
+int rebuild(fdtd_batch *b)
+{
+    std::vector<BatchDesc> descs(b->solves.size());
+    std::vector<BatchMurBlock> mur;
+    int units = 0;
+    const int ty = fused_tile_height();
+    for (size_t i = 0; i < b->solves.size(); i++) {
+        BatchSolve *v = b->solves[i];
+        BatchDesc &d = descs[i];
+        std::memset(&d, 0, sizeof d);
+        for (int par = 0; par < 2; par++) {
+            d.c[par] = solve_consts(v, par);
+            if (!encode_fused_maps(d.c[par], &d.maps[par]))
+                return FDTD_ERR_INVALID;
+        }
+        d.zchunk = fused_zchunk(v->nz);
+        d.tiles_x = (v->nx + 31) / 32;
+        d.tiles_y = (v->ny + ty - 1) / ty;
+        d.chunks = (v->nz + d.zchunk - 1) / d.zchunk;
+        d.unit_begin = units;
+        d.unit_count = d.tiles_x * d.tiles_y * d.chunks;
+        d.steps_target = v->steps_target;
+        units += d.unit_count;
+        for (int f = 0; f < 12; f++) {
+            const MurFace m = mur_face(f, v->nx, v->ny, v->nz);
+            const long long cells = (long long)m.len_u * m.len_v;
+            for (long long first = 0; first < cells; first += 256)
+                mur.push_back(BatchMurBlock{(int)i, f, (int)first, 0});
+        }
+    }
+    int st = FDTD_OK;
+    if (descs.size() > b->descs_cap) {
+        cudaFree(b->d_descs);
+        b->d_descs = nullptr;
+        st = cu(cudaMalloc(&b->d_descs, sizeof(BatchDesc) * descs.size()));
+        b->descs_cap = st == FDTD_OK ? descs.size() : 0;
+    }
+    if (st == FDTD_OK && mur.size() > b->mur_cap) {
+        cudaFree(b->d_mur);
+        b->d_mur = nullptr;
+        st = cu(cudaMalloc(&b->d_mur, sizeof(BatchMurBlock) * mur.size()));
+        b->mur_cap = st == FDTD_OK ? mur.size() : 0;
+    }
+    if (st == FDTD_OK && !descs.empty())
+        st = cu(cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(BatchDesc) * descs.size(), cudaMemcpyHostToDevice,
+                                b->stream));
+    if (st == FDTD_OK && !mur.empty())
+        st = cu(cudaMemcpyAsync(b->d_mur, mur.data(), sizeof(BatchMurBlock) * mur.size(), cudaMemcpyHostToDevice,
+                                b->stream));
+    if (st == FDTD_OK)
+        st = cu(cudaStreamSynchronize(b->stream));
+    if (st != FDTD_OK)
+        return st;
+    b->launch = BatchLaunch{b->d_descs, (int)descs.size(), units, b->d_work, b->d_mur, (int)mur.size(),
+                            batch_persistent_ctas()};
+    drop_graphs(b);
+    b->dirty = false;
+    return FDTD_OK;
+}
+
+int graph_for(fdtd_batch *b, int len, cudaGraphExec_t *out)
+{
+    auto it = b->graphs.find(len);
+    if (it != b->graphs.end()) {
+        *out = it->second;
+        return FDTD_OK;
+    }
+    int st = cu(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    if (st != FDTD_OK)
+        return st;
+    for (int k = 0; k < len && st == FDTD_OK; k++)
+        st = launch_batch_step(b->launch, b->stream);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (st != FDTD_OK || e != cudaSuccess) {
+        if (g)
+            cudaGraphDestroy(g);
+        return st != FDTD_OK ? st : (int)e;
+    }
+    cudaGraphExec_t exec = nullptr;
+    st = cu(cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+    if (st != FDTD_OK)
+        return st;
+    b->graphs[len] = exec;
+    *out = exec;
+    return FDTD_OK;
+}
+
+BatchSolve *find(fdtd_batch *b, int id)
+{
+    for (auto *v : b->solves)
+        if (v->id == id)
+            return v;
+    return nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t fdtd_batch_solve_bytes(int nx, int ny, int nz)
+{
+    if (nx < 3 || ny < 3 || nz < 3)
+        return 0;
+    // state + plan (class table, source table, Mur slabs)
+    return state_bytes(nx, ny, nz) + 256 * 32 + 65536 * 4 +
+           4 * 2 * ((size_t)ny * nz + (size_t)nx * nz + (size_t)nx * ny) + 6 * 256 + 256;
+}
+
+int fdtd_batch_create(int device, fdtd_batch **out)
+{
+    if (!out)
+        return FDTD_ERR_INVALID;
+    int st = cu(cudaSetDevice(device));
+    if (st != FDTD_OK)
+        return st;
+    auto *b = new (std::nothrow) fdtd_batch();
+    if (!b)
+        return FDTD_ERR_NOMEM;
+    b->device = device;
+    st = cu(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    if (st == FDTD_OK)
+        st = cu(cudaMalloc(&b->d_work, 256));
+    if (st == FDTD_OK)
+        st = cu(cudaMemset(b->d_work, 0, 256));
+    if (st != FDTD_OK) {
+        fdtd_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return FDTD_OK;
+}
+
+int fdtd_batch_destroy(fdtd_batch *b)
+{
+    if (!b)
+        return FDTD_OK;
+    cudaSetDevice(b->device);
+    if (b->stream)
+        cudaStreamSynchronize(b->stream);
+    drop_graphs(b);
+    for (auto *v : b->solves)
+        free_solve(v);
+    cudaFree(b->d_descs);
+    cudaFree(b->d_mur);
+    cudaFree(b->d_work);
+    if (b->stream)
+        cudaStreamDestroy(b->stream);
+    delete b;
+    return FDTD_OK;
+}
+
+int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int *id_out)
+{
+    if (!b || !cfg || !cfg->params || !cfg->material || !cfg->specs || steps < 0 || !id_out)
+        return FDTD_ERR_INVALID;
+    const FdtdParams *p = cfg->params;
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3)
+        return FDTD_ERR_INVALID;
+    int st = cu(cudaSetDevice(b->device));
+    if (st == FDTD_OK)
+        st = cu(cudaStreamSynchronize(b->stream));
+    if (st != FDTD_OK)
+        return st;
+    const size_t dense = (size_t)p->nx * p->ny * p->nz;
+    for (size_t i = 0; i < dense; i++)
+        if (cfg->material[i] >= cfg->nclasses)
+            return FDTD_ERR_INVALID;
+    auto *v = new (std::nothrow) BatchSolve();
+    if (!v)
+        return FDTD_ERR_NOMEM;
+    v->nx = p->nx; v->ny = p->ny; v->nz = p->nz;
+    v->pitch = (int)padded_pitch(p->nx);
+    v->ncell = (size_t)v->pitch * v->ny * v->nz;
+    v->steps_target = steps;
+    st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &v->plan);
+    const size_t fbytes = (v->ncell * sizeof(float) + 255) & ~size_t(255);
+    const size_t total = state_bytes(p->nx, p->ny, p->nz);
+    if (st == FDTD_OK)
+        st = cu(cudaMalloc(&v->d_block, total));
+    if (st == FDTD_OK)
+        st = cu(cudaMemsetAsync(v->d_block, 0, total, b->stream));
+    if (st == FDTD_OK) {
+        char *q = v->d_block;
+        for (int s = 0; s < 2; s++)
+            for (int k = 0; k < 3; k++, q += fbytes)
+                v->h[s][k] = reinterpret_cast<float *>(q);
+        for (int s = 0; s < 2; s++)
+            for (int k = 0; k < 3; k++, q += fbytes)
+                v->e[s][k] = reinterpret_cast<float *>(q);
+        for (int s = 0; s < 2; s++)
+            for (int k = 0; k < 3; k++, q += fbytes)
+                v->d[s][k] = reinterpret_cast<float *>(q);
+        v->mat = reinterpret_cast<uint8_t *>(q);
+        q += (v->ncell + 255) & ~size_t(255);
+        v->counter = reinterpret_cast<int *>(q);
+        // dense host classes -> padded rows (one 2-D copy per z plane range)
+        st = cu(cudaMemcpy2DAsync(v->mat, v->pitch, cfg->material, p->nx, p->nx, (size_t)p->ny * p->nz,
+                                  cudaMemcpyHostToDevice, b->stream));
+    }
+    if (st == FDTD_OK)
+        st = cu(cudaStreamSynchronize(b->stream));
+    if (st != FDTD_OK) {
+        free_solve(v);
+        return st;
+    }
+    v->bytes = total + fdtd_batch_solve_bytes(p->nx, p->ny, p->nz) - state_bytes(p->nx, p->ny, p->nz);
+    v->id = b->next_id++;
+    b->solves.push_back(v);
+    b->bytes += v->bytes;
+    b->dirty = true;
+    *id_out = v->id;
+    return FDTD_OK;
+}
+
+int fdtd_batch_remove(fdtd_batch *b, int id)
+{
+    if (!b)
+        return FDTD_ERR_INVALID;
+    BatchSolve *v = find(b, id);
+    if (!v)
+        return FDTD_ERR_INVALID;
+    cudaSetDevice(b->device);
+    const int st = cu(cudaStreamSynchronize(b->stream));
+    b->solves.erase(std::find(b->solves.begin(), b->solves.end(), v));
+    b->bytes -= v->bytes;
+    free_solve(v);
+    b->dirty = true;
+    return st;
+}
+
+int fdtd_batch_run(fdtd_batch *b, int nsteps)
+{
+    if (!b || nsteps < 0)
+        return FDTD_ERR_INVALID;
+    int st = cu(cudaSetDevice(b->device));
+    if (st != FDTD_OK || nsteps == 0 || b->solves.empty())
+        return st;
+    if (b->dirty && (st = rebuild(b)) != FDTD_OK)
+        return st;
+    const int chunk = 8;
+    while (nsteps > 0 && st == FDTD_OK) {
+        const int len = nsteps >= chunk ? chunk : 1;
+        cudaGraphExec_t g;
+        st = graph_for(b, len, &g);
+        if (st == FDTD_OK)
+            st = cu(cudaGraphLaunch(g, b->stream));
+        nsteps -= len;
+    }
+    return st;
+}
+
+int fdtd_batch_synchronize(fdtd_batch *b)
+{
+    if (!b)
+        return FDTD_ERR_INVALID;
+    cudaSetDevice(b->device);
+    int st = cu(cudaStreamSynchronize(b->stream));
+    for (auto *v : b->solves)
+        if (st == FDTD_OK)
+            st = plan_error(v->plan);
+    return st;
+}
+
+int fdtd_batch_steps(fdtd_batch *b, int id)
+{
+    if (!b)
+        return -1;
+    BatchSolve *v = find(b, id);
+    if (!v || fdtd_batch_synchronize(b) != FDTD_OK)
+        return -1;
+    int n = -1;
+    if (cudaMemcpy(&n, v->counter, sizeof n, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return -1;
+    return n;
+}
+
+int fdtd_batch_get_field(fdtd_batch *b, int id, int field, int z0, int nplanes, float *host_out)
+{
+    if (!b || !host_out || field < 0 || field >= FDTD_FIELD_COUNT)
+        return FDTD_ERR_INVALID;
+    BatchSolve *v = find(b, id);
+    if (!v)
+        return FDTD_ERR_INVALID;
+    if (nplanes == 0) {
+        z0 = 0;
+        nplanes = v->nz;
+    }
+    if (z0 < 0 || nplanes < 0 || z0 + nplanes > v->nz)
+        return FDTD_ERR_INVALID;
+    int st = fdtd_batch_synchronize(b);
+    int n = 0;
+    if (st == FDTD_OK)
+        st = cu(cudaMemcpy(&n, v->counter, sizeof n, cudaMemcpyDeviceToHost));
+    if (st != FDTD_OK)
+        return st;
+    const int comp = field % 3;
+    const float *src;
+    if (field < 3)
+        src = v->h[n & 1][comp];
+    else {
+        const int slot = n > 0 ? ((n - 1) & 1) : 0;
+        src = field < 6 ? v->d[slot][comp] : v->e[slot][comp];
+    }
+    src += (size_t)z0 * v->pitch * v->ny;
+    return cu(cudaMemcpy2D(host_out, sizeof(float) * v->nx, src, sizeof(float) * v->pitch, sizeof(float) * v->nx,
+                           (size_t)v->ny * nplanes, cudaMemcpyDeviceToHost));
+}
+
+size_t fdtd_batch_bytes(const fdtd_batch *b) { return b ? b->bytes : 0; }
+
+int fdtd_batch_size(const fdtd_batch *b) { return b ? (int)b->solves.size() : 0; }
+
+fdtd_stream_t fdtd_batch_stream(const fdtd_batch *b) { return b ? b->stream : nullptr; }
+
+}  // extern "C"

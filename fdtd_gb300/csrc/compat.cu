@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) compat_mur_kernel(MurArgs a)
     if (idx >= (long long)m.len_u * m.len_v)
         return;
     const int iu = (int)(idx % m.len_u), iv = (int)(idx / m.len_u);
-    mur_apply(f, iu, iv, nx, ny, nz, c_sym.dt, c_sym.dx, c_sym.dy, c_sym.dz, c_sym.mu0 * c_sym.eps0, a.rp, a.t[0],
+    mur_apply(f, iu, iv, nx, ny, nz, nx, c_sym.dt, c_sym.dx, c_sym.dy, c_sym.dz, c_sym.mu0 * c_sym.eps0, a.rp, a.t[0],
               a.t[1], a.t[2], a.s[0], a.s[1], a.s[2], false);
 }
 

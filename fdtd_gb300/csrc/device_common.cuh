@@ -96,10 +96,12 @@ struct MurSlabs {
     const float *rpx0, *rpy0, *rpz0, *rpx_end, *rpy_end, *rpz_end;
 };
 
-// Applies updateMurBoundary to face set f, in-face position (iu, iv).
+// Applies updateMurBoundary to face set f, in-face position (iu, iv); pitch
+// is the row stride of the E arrays (nx when dense).
 // eT: E^{n+1} (written), eS: E^n.  fix_ey selects the corrected scheme's
 // E^{n+1} term on the ey x = nx-1 face (the reference reads E^n there, :323).
-__device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny, int nz, float dt, float hx, float hy,
+__device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny, int nz, int pitch, float dt, float hx,
+                                          float hy,
                                           float hz, float me, const MurSlabs &rp, float *t0, float *t1, float *t2,
                                           const float *s0, const float *s1, const float *s2, bool fix_ey)
 {
@@ -126,8 +128,8 @@ __device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny,
         rs = slab[((size_t)(m.far ? 1 : 0) * ny + y) * nx + x];
         rn = slab[((size_t)(m.far ? 0 : 1) * ny + y) * nx + x];
     }
-    const size_t i = cell_index(x, y, z, nx, ny);
-    const size_t j = cell_index(x + dxn, y + dyn, z + dzn, nx, ny);
+    const size_t i = cell_index(x, y, z, pitch, ny);
+    const size_t j = cell_index(x + dxn, y + dyn, z + dzn, pitch, ny);
     // component pointers picked with selects (an indexed array would live in local memory)
     const float *S = m.comp == 0 ? s0 : (m.comp == 1 ? s1 : s2);
     float *T = m.comp == 0 ? t0 : (m.comp == 1 ? t1 : t2);

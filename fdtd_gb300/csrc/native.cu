@@ -42,6 +42,7 @@ NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)
     c.nx = p->nx;
     c.ny = p->ny;
     c.nz = p->nz;
+    c.pitch = p->nx;
     c.kx = p->dt / (p->mu0 * p->dx);
     c.ky = p->dt / (p->mu0 * p->dy);
     c.kz = p->dt / (p->mu0 * p->dz);
@@ -203,7 +204,7 @@ __global__ void __launch_bounds__(256) native_mur_kernel(NativeConsts c)
         atomicAdd(c.step_counter, 1);
     if (idx >= (long long)m.len_u * m.len_v)
         return;
-    mur_apply(f, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.dt, c.hx, c.hy, c.hz, c.me, c.rp,
+    mur_apply(f, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz, c.me, c.rp,
               c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
               c.scheme == FDTD_SCHEME_CORRECTED);
 }

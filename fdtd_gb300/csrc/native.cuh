@@ -1,6 +1,8 @@
 // native.cuh -- plan object and kernel argument block of the native path.
 #pragma once
 
+#include <cuda.h>
+
 #include <vector>
 
 #include "device_common.cuh"
@@ -27,6 +29,7 @@ namespace fdtd {
 // Kernel argument block (passed by value).
 struct NativeConsts {
     int nx, ny, nz;
+    int pitch;             // elements between consecutive rows (nx for dense arrays)
     float kx, ky, kz;      // dt / (mu0 d{x,y,z}) of the H update
     float tx, ty, tz;      // dt / d{x,y,z} of the D update
     float dt, hx, hy, hz;  // time step and cell sizes (Mur)
@@ -70,6 +73,48 @@ int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int ma
 // H, D, sources and E of one step in the single-pass kernel (the Mur faces
 // follow in launch_mur).
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s);
+
+// Tensor maps of one single-pass launch: E^n (3), H_old (3), D^n (3),
+// D^{n-1} (3), E^{n-1} (3), material classes (1).
+struct FusedMaps {
+    CUtensorMap m[16];
+};
+
+// One solve of a batch as the batched kernels see it (device memory).  The
+// solve's completed-step count n selects c[n & 1] / maps[n & 1]; units
+// [unit_begin, unit_begin + unit_count) are its (tile x, tile y, z chunk)
+// work items; it is skipped once n reaches steps_target.
+struct alignas(64) BatchDesc {
+    FusedMaps maps[2];
+    NativeConsts c[2];
+    int zchunk, tiles_x, tiles_y, chunks;
+    int unit_begin, unit_count;
+    int steps_target;
+    int pad;
+};
+
+// One face block of the batched Mur launch: solve, face set, first cell.
+struct BatchMurBlock {
+    int solve, face, first, pad;
+};
+
+struct BatchLaunch {
+    const BatchDesc *descs;
+    int nsolves;
+    int total_units;
+    int *work_counter;
+    const BatchMurBlock *mur_blocks;
+    int nmur_blocks;
+    int persistent_ctas;
+};
+
+// Tensor maps of a single-pass launch over c's buffers (false: not encodable).
+bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps);
+int fused_tile_height();
+int fused_zchunk(int nz);
+// One batched step: fused kernel over all units, Mur faces, step counters.
+int launch_batch_step(const BatchLaunch &b, cudaStream_t s);
+int batch_persistent_ctas();
 
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);

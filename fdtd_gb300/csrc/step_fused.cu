@@ -53,12 +53,6 @@ struct Geo {
     static constexpr unsigned TX_EPI = 3u * E_BYTES;
 };
 
-// Tensor maps of one launch: E^n (3), H_old (3), D^n (3), D^{n-1} (3),
-// E^{n-1} (3), material (1).
-struct FusedMaps {
-    CUtensorMap m[16];
-};
-
 struct FusedArgs {
     NativeConsts c;
     int zchunk;
@@ -158,13 +152,13 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
 {
     using G = Geo<TY>;
     constexpr int NT = FTX * TY;
-    const int nx = c.nx, ny = c.ny;
-    const size_t plane = (size_t)nx * ny;
+    const int nx = c.nx, ny = c.ny, pitch = c.pitch;
+    const size_t plane = (size_t)pitch * ny;
     auto box = [&](const float *base, uint32_t dst, int xs, int ys, int w, int h) {
         for (int i = tid; i < w * h; i += NT) {
             const int gx = xs + i % w, gy = ys + i / w;
             const bool ok = gx >= 0 && gx < nx && gy >= 0 && gy < ny;
-            const float *src = ok ? base + (size_t)z * plane + (size_t)gy * nx + gx : base;
+            const float *src = ok ? base + (size_t)z * plane + (size_t)gy * pitch + gx : base;
             cp_async4(dst + 4u * i, src, ok);
         }
     };
@@ -184,41 +178,28 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
 
 // ---------------------------------------------------------------- the kernel
 
+// One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
+// stage ring and its barriers continue from earlier units of the same CTA:
+// g0 counts the planes this CTA has staged before.  Returns false when a
+// bounded wait gave up (the error flag is set; the CTA must stop).
 template <int TY, int S, bool TMA>
-__global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
-                                                             const __grid_constant__ FusedMaps maps)
+__device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMaps &maps, int zchunk, int bx, int by,
+                                           int bz, unsigned char *smem, const DebyeCoef *coef, uint64_t *bars,
+                                           unsigned g0)
 {
     using G = Geo<TY>;
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    // TMA destinations want 128-byte alignment; the launch adds 128 bytes of slack
-    unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
-    const NativeConsts &c = a.c;
     const int nx = c.nx, ny = c.ny, nz = c.nz;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FTX + tx;
-    const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * TY;
+    const int x0 = bx * FTX, y0 = by * TY;
     const int x = x0 + tx, y = y0 + ty;
-    const int zc0 = blockIdx.z * a.zchunk, zc1 = min(nz, zc0 + a.zchunk);
+    const int zc0 = bz * zchunk, zc1 = min(nz, zc0 + zchunk);
     const int p0 = max(zc0 - 1, 0), plast = min(zc1, nz - 1);
     const int nplanes = plast - p0 + 1;
 
     float *hn = reinterpret_cast<float *>(smem + S * G::STAGE);
-    DebyeCoef *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + c.nclasses * sizeof(DebyeCoef));
-    auto stage = [&](int k) { return smem + (k % S) * G::STAGE; };
-
-    // coefficient table -> shared memory
-    {
-        const float *src = reinterpret_cast<const float *>(c.coef);
-        float *dst = reinterpret_cast<float *>(coef);
-        for (int i = tid; i < c.nclasses * 8; i += FTX * TY)
-            dst[i] = src[i];
-    }
-    if (TMA && tid == 0) {
-        for (int s = 0; s < S; s++)
-            mbar_init(smem_addr(&bars[s]), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
+    auto stage = [&](int k) { return smem + ((g0 + k) % S) * G::STAGE; };
+    auto bar = [&](int k) { return smem_addr(&bars[(g0 + k) % S]); };
+    auto parity = [&](int k) { return ((g0 + k) / S) & 1u; };
 
     // prologue: fill the ring
     for (int k = 0; k < S; k++) {
@@ -226,7 +207,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             const int z = p0 + k;
             if (TMA) {
                 if (tid == 0)
-                    issue_plane_tma<TY>(maps, stage(k), smem_addr(&bars[k % S]), plane_kind<TY>(z, zc0, zc1), x0, y0, z);
+                    issue_plane_tma<TY>(maps, stage(k), bar(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z);
             } else {
                 issue_plane_generic<TY>(c, stage(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z, tid);
             }
@@ -244,8 +225,8 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     }
 
     const bool in_dom = x < nx && y < ny;
-    const size_t plane = (size_t)nx * ny;
-    const size_t col = (size_t)y * nx + x;
+    const size_t plane = (size_t)c.pitch * ny;  // elements between z planes
+    const size_t col = (size_t)y * c.pitch + x;
     const float kx = c.kx, ky = c.ky, kz = c.kz, tcx = c.tx, tcy = c.ty, tcz = c.tz;
     float hxm = 0.0f, hym = 0.0f;  // H^{n+1/2} of this column at z-1
     uint8_t mat_next = 0;
@@ -260,19 +241,19 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
         if (TMA) {
             bool ok = true;
             if (k == 0)
-                ok = mbar_wait(smem_addr(&bars[0]), 0);
+                ok = mbar_wait(bar(0), parity(0));
             if (ok && k + 1 < nplanes)
-                ok = mbar_wait(smem_addr(&bars[(k + 1) % S]), ((k + 1) / S) & 1);
+                ok = mbar_wait(bar(k + 1), parity(k + 1));
             // one decision for the whole CTA, so no thread is left at a barrier
             if (__syncthreads_or(!ok)) {
                 if (tid == 0) {
                     atomicExch(c.err, 1);
                     // let the copies in flight land before the CTA exits (bounded)
                     for (int j = k; j < nplanes && j < k + S; j++)
-                        mbar_wait(smem_addr(&bars[j % S]), (j / S) & 1);
+                        mbar_wait(bar(j), parity(j));
                 }
                 __syncthreads();
-                return;
+                return false;
             }
         } else {
             cp_async_wait<S - 2>();
@@ -411,8 +392,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             if (tid == 0 && kn < nplanes) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const int zn = p0 + kn;
-                issue_plane_tma<TY>(maps, stage(kn), smem_addr(&bars[kn % S]), plane_kind<TY>(zn, zc0, zc1), x0, y0,
-                                    zn);
+                issue_plane_tma<TY>(maps, stage(kn), bar(kn), plane_kind<TY>(zn, zc0, zc1), x0, y0, zn);
             }
         } else {
             if (kn < nplanes) {
@@ -424,6 +404,149 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     }
     if (!TMA)
         cp_async_wait<0>();
+    return true;
+}
+
+// Shared-memory layout of a CTA: S stages, the H^{n+1/2} plane, the class
+// table (up to FDTD_MAX_CLASSES entries), S barriers.
+template <int TY, int S>
+__host__ __device__ constexpr int fused_smem_bytes(int nclasses)
+{
+    return 128 + S * Geo<TY>::STAGE + Geo<TY>::HN_BYTES + nclasses * (int)sizeof(DebyeCoef) + S * 8;
+}
+
+template <int TY, int S, bool TMA>
+__device__ __forceinline__ void fused_cta_setup(unsigned char *smem, DebyeCoef **coef, uint64_t **bars)
+{
+    using G = Geo<TY>;
+    *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
+    *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * sizeof(DebyeCoef));
+    const int tid = threadIdx.y * FTX + threadIdx.x;
+    if (TMA && tid == 0) {
+        for (int s = 0; s < S; s++)
+            mbar_init(smem_addr(&(*bars)[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+}
+
+__device__ __forceinline__ void load_coef(const NativeConsts &c, DebyeCoef *coef, int nthreads)
+{
+    const float *src = reinterpret_cast<const float *>(c.coef);
+    float *dst = reinterpret_cast<float *>(coef);
+    const int tid = threadIdx.y * FTX + threadIdx.x;
+    for (int i = tid; i < c.nclasses * 8; i += nthreads)
+        dst[i] = src[i];
+}
+
+// One solve: CTA (bx, by, bz) processes one unit.
+template <int TY, int S, bool TMA>
+__global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
+                                                             const __grid_constant__ FusedMaps maps)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    DebyeCoef *coef;
+    uint64_t *bars;
+    fused_cta_setup<TY, S, TMA>(smem, &coef, &bars);
+    load_coef(a.c, coef, FTX * TY);
+    __syncthreads();
+    fused_unit<TY, S, TMA>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, blockIdx.z, smem, coef, bars, 0u);
+}
+
+// Many solves: persistent CTAs take work units from a counter; a unit's solve
+// descriptor supplies the constants (copied to shared memory) and tensor maps
+// (read by TMA from device memory).  Units of finished solves are skipped.
+template <int TY, int S>
+__global__ void __launch_bounds__(FTX *TY) batch_step_kernel(const BatchDesc *__restrict__ descs, int nsolves,
+                                                             int total_units, int *work_counter)
+{
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
+    __shared__ NativeConsts s_c;
+    __shared__ int s_unit, s_solve;
+    DebyeCoef *coef;
+    uint64_t *bars;
+    fused_cta_setup<TY, S, true>(smem, &coef, &bars);
+    const int tid = threadIdx.y * FTX + threadIdx.x;
+    int loaded = -1;
+    unsigned g = 0;
+    __syncthreads();
+    for (;;) {
+        if (tid == 0) {
+            const int u = atomicAdd(work_counter, 1);
+            int lo = 0, hi = nsolves - 1;
+            if (u < total_units) {
+                while (lo < hi) {  // last solve with unit_begin <= u
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (descs[mid].unit_begin <= u)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+            }
+            s_unit = u;
+            s_solve = lo;
+        }
+        __syncthreads();
+        const int u = s_unit, sv = s_solve;
+        if (u >= total_units)
+            break;
+        const BatchDesc &d = descs[sv];
+        const int n = *d.c[0].step_counter;
+        if (n < d.steps_target) {
+            const int par = n & 1;
+            {
+                const int *src = reinterpret_cast<const int *>(&d.c[par]);
+                int *dst = reinterpret_cast<int *>(&s_c);
+                for (int i = tid; i < (int)(sizeof(NativeConsts) / 4); i += FTX * TY)
+                    dst[i] = src[i];
+            }
+            if (sv != loaded)
+                load_coef(d.c[par], coef, FTX * TY);
+            __syncthreads();
+            loaded = sv;
+            const int local = u - d.unit_begin;
+            const int per_z = d.tiles_x * d.tiles_y;
+            const int bz = local / per_z, rem = local % per_z;
+            const int by = rem / d.tiles_x, bx = rem % d.tiles_x;
+            const int zc0 = bz * d.zchunk, zc1 = min(s_c.nz, zc0 + d.zchunk);
+            const int nplanes = min(zc1, s_c.nz - 1) - max(zc0 - 1, 0) + 1;
+            if (!fused_unit<TY, S, true>(s_c, d.maps[par], d.zchunk, bx, by, bz, smem, coef, bars, g))
+                return;
+            g += (unsigned)nplanes;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) batch_mur_kernel(const BatchDesc *__restrict__ descs,
+                                                        const BatchMurBlock *__restrict__ blocks)
+{
+    const BatchMurBlock b = blocks[blockIdx.x];
+    const BatchDesc &d = descs[b.solve];
+    const int n = *d.c[0].step_counter;
+    if (n >= d.steps_target)
+        return;
+    const NativeConsts &c = d.c[n & 1];
+    const MurFace m = mur_face(b.face, c.nx, c.ny, c.nz);
+    const long long idx = (long long)b.first + threadIdx.x;
+    if (idx >= (long long)m.len_u * m.len_v)
+        return;
+    mur_apply(b.face, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz,
+              c.me, c.rp, c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
+              c.scheme == FDTD_SCHEME_CORRECTED);
+}
+
+__global__ void batch_advance_kernel(const BatchDesc *__restrict__ descs, int nsolves, int *work_counter)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s == 0)
+        *work_counter = 0;
+    if (s < nsolves) {
+        int *ctr = descs[s].c[0].step_counter;
+        if (*ctr < descs[s].steps_target)
+            *ctr += 1;
+    }
 }
 
 // ------------------------------------------------------------------ host side
@@ -447,11 +570,11 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
 }
 
 bool encode_map(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void *base, bool is_u8, int nx, int ny,
-                int nz, int bx, int by)
+                int nz, int pitch, int bx, int by)
 {
     const size_t es = is_u8 ? 1 : 4;
     cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-    cuuint64_t strides[2] = {(cuuint64_t)(nx * es), (cuuint64_t)((size_t)nx * ny * es)};
+    cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)((size_t)pitch * ny * es)};
     cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     const CUresult r =
@@ -468,7 +591,7 @@ int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
     using G = Geo<TY_SEL>;
     auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA>;
-    const int smem = 128 + S_SEL * G::STAGE + G::HN_BYTES + a.c.nclasses * (int)sizeof(DebyeCoef) + S_SEL * 8;
+    const int smem = fused_smem_bytes<TY_SEL, S_SEL>(FDTD_MAX_CLASSES);
     static std::once_flag once;
     std::call_once(once, [&] {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -493,13 +616,67 @@ int fused_zchunk(int nz)
 
 bool fused_uses_tma(const NativeConsts &c)
 {
-    if (c.nx % 16 != 0 || !encode_fn())
+    if (c.pitch % 16 != 0 || !encode_fn())
         return false;
     for (int k = 0; k < 3; k++)
         if (!aligned16(c.e_cur[k]) || !aligned16(c.h_in[k]) || !aligned16(c.d_cur[k]) || !aligned16(c.d_prev[k]) ||
             !aligned16(c.e_prev[k]))
             return false;
     return aligned16(c.mat);
+}
+
+bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps)
+{
+    memset(maps, 0, sizeof *maps);
+    if (!fused_uses_tma(c))
+        return false;
+    auto fn = encode_fn();
+    using G = Geo<TY_SEL>;
+    bool ok = true;
+    for (int k = 0; k < 3 && ok; k++) {
+        ok &= encode_map(fn, &maps->m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, c.pitch, G::EW, G::EH);
+        ok &= encode_map(fn, &maps->m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, c.pitch, G::HW, G::HH);
+        ok &= encode_map(fn, &maps->m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+        ok &= encode_map(fn, &maps->m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+        ok &= encode_map(fn, &maps->m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+    }
+    return ok && encode_map(fn, &maps->m[15], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+}
+
+int fused_tile_height() { return TY_SEL; }
+
+int batch_persistent_ctas()
+{
+    static int ctas = 0;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        auto kernel = batch_step_kernel<TY_SEL, S_SEL>;
+        const int smem = fused_smem_bytes<TY_SEL, S_SEL>(FDTD_MAX_CLASSES);
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FTX * TY_SEL, smem);
+        ctas = sms * (per_sm > 0 ? per_sm : 1);
+    });
+    return ctas;
+}
+
+int launch_batch_step(const BatchLaunch &b, cudaStream_t s)
+{
+    const int smem = fused_smem_bytes<TY_SEL, S_SEL>(FDTD_MAX_CLASSES);
+    batch_step_kernel<TY_SEL, S_SEL><<<b.persistent_ctas, dim3(FTX, TY_SEL), smem, s>>>(b.descs, b.nsolves,
+                                                                                         b.total_units, b.work_counter);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && b.nmur_blocks > 0) {
+        batch_mur_kernel<<<b.nmur_blocks, 256, 0, s>>>(b.descs, b.mur_blocks);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        batch_advance_kernel<<<(b.nsolves + 255) / 256, 256, 0, s>>>(b.descs, b.nsolves, b.work_counter);
+        e = cudaGetLastError();
+    }
+    return e == cudaSuccess ? FDTD_OK : (int)e;
 }
 
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
@@ -517,13 +694,13 @@ int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
         using G = Geo<TY_SEL>;
         bool ok = true;
         for (int k = 0; k < 3 && ok; k++) {
-            ok &= encode_map(fn, &maps.m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, G::EW, G::EH);
-            ok &= encode_map(fn, &maps.m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, G::HW, G::HH);
-            ok &= encode_map(fn, &maps.m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
-            ok &= encode_map(fn, &maps.m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
-            ok &= encode_map(fn, &maps.m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, c.pitch, G::EW, G::EH);
+            ok &= encode_map(fn, &maps.m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, c.pitch, G::HW, G::HH);
+            ok &= encode_map(fn, &maps.m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+            ok &= encode_map(fn, &maps.m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
         }
-        ok &= encode_map(fn, &maps.m[15], c.mat, true, c.nx, c.ny, c.nz, FTX, TY_SEL);
+        ok &= encode_map(fn, &maps.m[15], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
         if (ok)
             return launch_fused_impl<true>(a, maps, s);
     }

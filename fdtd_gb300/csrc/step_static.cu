@@ -117,6 +117,7 @@ extern "C" int fdtd_step_static(const FdtdParams *p, const float *specs, int ncl
 
     NativeConsts c{};
     c.nx = p->nx; c.ny = p->ny; c.nz = p->nz;
+    c.pitch = p->nx;
     c.kx = p->dt / (p->mu0 * p->dx);
     c.ky = p->dt / (p->mu0 * p->dy);
     c.kz = p->dt / (p->mu0 * p->dz);

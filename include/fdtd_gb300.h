@@ -381,6 +381,38 @@ int fdtd_solver_profile(fdtd_solver *s, int nsteps, float *avg_ms, int max_kerne
 /* Name of kernel k of a step, as reported by fdtd_solver_profile. */
 const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k);
 
+/* ------------------------------------------------------------------------
+ * Batch: many independent solves of uneven sizes advanced together (no
+ * reference counterpart).  Each solve keeps its own resident state and plan;
+ * one batched step is a persistent kernel over the column-tile x z-chunk work
+ * units of every solve, one Mur launch over every solve's face cells and a
+ * counter advance, replayed as a CUDA graph.  A solve stops at its own step
+ * target; adding or removing a solve rebuilds the launch.  Results of a solve
+ * are identical whether it runs alone or with others.
+ * ---------------------------------------------------------------------- */
+
+typedef struct fdtd_batch fdtd_batch;
+
+int fdtd_batch_create(int device, fdtd_batch **out);
+int fdtd_batch_destroy(fdtd_batch *b);
+/* Device bytes one solve of this grid needs (state + plan), for admission. */
+size_t fdtd_batch_solve_bytes(int nx, int ny, int nz);
+/* Adds a solve (cfg->kernel and cfg->device are ignored) that will run
+ * `steps` steps; *id receives its handle. */
+int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int *id);
+int fdtd_batch_remove(fdtd_batch *b, int id);
+/* Enqueues nsteps batched steps (asynchronous). */
+int fdtd_batch_run(fdtd_batch *b, int nsteps);
+int fdtd_batch_synchronize(fdtd_batch *b);
+/* Completed steps of one solve (synchronises; -1 on error). */
+int fdtd_batch_steps(fdtd_batch *b, int id);
+/* Copies planes [z0, z0 + nplanes) (nplanes 0 = all) of one field of one
+ * solve into host memory, nx*ny*nplanes floats. */
+int fdtd_batch_get_field(fdtd_batch *b, int id, int field, int z0, int nplanes, float *host_out);
+size_t fdtd_batch_bytes(const fdtd_batch *b);
+int fdtd_batch_size(const fdtd_batch *b);
+fdtd_stream_t fdtd_batch_stream(const fdtd_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

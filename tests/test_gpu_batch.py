@@ -1,0 +1,85 @@
+"""Batched solves (fdtd_batch_*): every solve of a mixed batch equals the same
+solve run alone and the oracle, including solves added while others run."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import fdtd_gb300 as fg
+from oracle import pyoracle as po
+
+from .gpu_util import Params, make_params
+from .helpers import assert_fields_close, class_media, random_case
+
+pytestmark = pytest.mark.gpu
+
+CASES = [  # dims, steps, scheme
+    ((48, 37, 29), 30, fg.SCHEME_REFERENCE),
+    ((64, 64, 40), 45, fg.SCHEME_CORRECTED),
+    ((33, 50, 70), 20, fg.SCHEME_REFERENCE),
+    ((96, 20, 16), 60, fg.SCHEME_CORRECTED),
+    ((17, 9, 11), 12, fg.SCHEME_REFERENCE),
+]
+
+
+def _case(k):
+    dims, steps, scheme = CASES[k]
+    codes, specs, rp, sources, consts, jz = random_case(*dims, seed=100 + k, ncls=4, nsrc=2)
+    raw = make_params(dims, consts, sources, jz, default=(0.0, 1.0, 1.0, 0.0))
+    return dims, steps, scheme, codes, specs, sources, consts, jz, raw
+
+
+def _oracle(dims, steps, scheme, codes, specs, sources, consts, jz, raw):
+    p = po.OracleParams()
+    p.nx, p.ny, p.nz = dims
+    p.pi, p.wave_frequency, p.eps0 = raw.pi, raw.waveFrequency, raw.eps0
+    p.default_sigma, p.default_eps_s = raw.defaultSigma, raw.defaultEpsS
+    p.default_eps_i, p.default_tau_d = raw.defaultEpsI, raw.defaultTauD
+    media = class_media(codes, specs, po.uniform_media(p).rp)
+    corrected = scheme == fg.SCHEME_CORRECTED
+    st = po.State(*dims, np.float64 if corrected else np.float32)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts, corrected=corrected), media, st, 0, steps)
+    return st.latest(steps)
+
+
+def test_mixed_batch_matches_lone_solves_and_oracle(cuda):
+    b = fg.Batch()
+    ids = []
+    cases = [_case(k) for k in range(len(CASES))]
+    for dims, steps, scheme, codes, specs, sources, consts, jz, raw in cases:
+        ids.append(b.add(Params(raw), codes, specs, steps, scheme=scheme))
+    assert len(b) == len(CASES)
+    b.run(max(c[1] for c in cases) + 5)  # every solve stops at its own target
+    for sid, case in zip(ids, cases):
+        dims, steps, scheme, codes, specs, sources, consts, jz, raw = case
+        assert b.steps(sid) == steps
+        got = b.fields(sid)
+        # alone: the single-solve path on the same inputs
+        with fg.Solver(Params(raw), codes, specs, scheme=scheme) as s:
+            s.run(steps)
+            alone = s.fields()
+        for name in got:
+            assert np.array_equal(got[name].view(np.uint32), alone[name].view(np.uint32)), (dims, name)
+        assert_fields_close(got, _oracle(*case))
+    b.close()
+
+
+def test_solves_added_and_removed_while_running(cuda):
+    b = fg.Batch()
+    c0, c1, c2 = _case(0), _case(1), _case(3)
+    i0 = b.add(Params(c0[8]), c0[3], c0[4], c0[1], scheme=c0[2])
+    i1 = b.add(Params(c1[8]), c1[3], c1[4], c1[1], scheme=c1[2])
+    b.run(10)
+    i2 = b.add(Params(c2[8]), c2[3], c2[4], c2[1], scheme=c2[2])
+    b.run(15)
+    b.remove(i0)  # finished or not, its memory is released
+    b.run(60)
+    assert b.steps(i1) == c1[1] and b.steps(i2) == c2[1]
+    for sid, case in ((i1, c1), (i2, c2)):
+        assert_fields_close(b.fields(sid), _oracle(*case))
+    b.close()
+
+
+def test_solve_bytes_accounts_state():
+    assert fg.Batch.solve_bytes(64, 64, 64) >= 73 * 64 ** 3
+    assert fg.Batch.solve_bytes(2, 64, 64) == 0

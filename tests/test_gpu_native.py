@@ -99,11 +99,10 @@ def test_single_pass_small_z_chunks(cuda, monkeypatch, dims, chunk):
     assert_fields_close(got, st.latest(steps))
 
 
-def test_single_pass_kernel_variants(cuda, monkeypatch, variant, dims, seed):
-    """Every tile/ring/Mur variant of the single-pass kernel against the FP32
-    oracle (TMA staging for nx % 16 == 0, cp.async otherwise)."""
-    for k, v in variant.items():
-        monkeypatch.setenv(k, v)
+@pytest.mark.parametrize("dims,seed", [((64, 40, 70), 12), ((48, 17, 9), 13), ((33, 26, 10), 14)])
+def test_single_pass_both_schemes(cuda, dims, seed):
+    """Single-pass kernel in both schemes (TMA staging for nx % 16 == 0,
+    cp.async otherwise) against the FP32 / FP64 oracle."""
     nx, ny, nz = dims
     codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, seed, nsrc=3)
     steps = 7
