@@ -42,6 +42,7 @@ SCHEME_REFERENCE = 0
 SCHEME_CORRECTED = 1
 KERNEL_SINGLE_PASS = 0
 KERNEL_TWO_PASS = 1
+KERNEL_COMPACT = 2      # nine stored fields (H, E, R); D is not readable
 FIELDS = ("hx", "hy", "hz", "dx", "dy", "dz", "ex", "ey", "ez")
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
@@ -303,6 +304,7 @@ class Solver:
         h = C.c_void_p()
         check(lib().fdtd_solver_create(C.byref(cfg), C.byref(h)), "fdtd_solver_create")
         self.handle = h
+        self.kernel = kernel
         self._cb = None
         self._spec = None
 
@@ -326,7 +328,9 @@ class Solver:
         return out
 
     def fields(self) -> dict[str, np.ndarray]:
-        return {n: self.field(n) for n in FIELDS}
+        """Every stored field (the compact form stores no D)."""
+        names = [n for n in FIELDS if not (self.kernel == KERNEL_COMPACT and n.startswith("d"))]
+        return {n: self.field(n) for n in names}
 
     def set_snapshots(self, every: int, fields=("ex", "ey", "ez"), z0: int = 0, nplanes: int = 0,
                       callback=None, output_dir: str | None = None, writer_threads: int = 0) -> None:

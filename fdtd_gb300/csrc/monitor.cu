@@ -319,10 +319,16 @@ struct CheckpointHeader {
 
 static const char CKP_MAGIC[8] = {'F', 'D', 'T', 'D', 'G', 'B', '3', 'C'};
 
-// The 15 state arrays after `count` steps: H, E^n, E^{n-1}, D^n, D^{n-1}.
+// Checkpoint versions: 1 holds the D form's 15 arrays (either D-form
+// kernel restores it), 2 the compact form's 12.
+static uint32_t ckp_version(const fdtd_solver *s) { return s->kernel == FDTD_KERNEL_COMPACT ? 2u : 1u; }
+static int ckp_arrays(const fdtd_solver *s) { return s->kernel == FDTD_KERNEL_COMPACT ? 12 : 15; }
+
+// The state arrays after `count` steps: H, E^n, E^{n-1}, then D^n, D^{n-1}
+// (D form) or R (compact form).
 static void state_arrays(fdtd_solver *s, int count, float *out[15])
 {
-    const int hb = s->kernel == FDTD_KERNEL_SINGLE_PASS ? (count & 1) : 0;
+    const int hb = s->kernel != FDTD_KERNEL_TWO_PASS ? (count & 1) : 0;
     const int l = latest_slot(count), p = previous_slot(count);
     for (int c = 0; c < 3; c++) {
         out[c] = s->h[hb][c];
@@ -345,7 +351,7 @@ int fdtd_solver_checkpoint(fdtd_solver *s, const char *path)
         return FDTD_ERR_IO;
     CheckpointHeader h{};
     std::memcpy(h.magic, CKP_MAGIC, 8);
-    h.version = 1;
+    h.version = ckp_version(s);
     h.nx = s->nx; h.ny = s->ny; h.nz = s->nz;
     h.scheme = s->scheme;
     h.nclasses = s->nclasses;
@@ -355,7 +361,7 @@ int fdtd_solver_checkpoint(fdtd_solver *s, const char *path)
     float *arrs[15];
     state_arrays(s, s->steps, arrs);
     std::vector<float> buf(s->ncell);
-    for (int k = 0; k < 15 && ok; k++) {
+    for (int k = 0; k < ckp_arrays(s) && ok; k++) {
         st = cu(cudaMemcpy(buf.data(), arrs[k], sizeof(float) * s->ncell, cudaMemcpyDeviceToHost));
         ok = st == FDTD_OK && std::fwrite(buf.data(), sizeof(float), s->ncell, f) == s->ncell;
     }
@@ -379,7 +385,7 @@ int fdtd_solver_restore(fdtd_solver *s, const char *path)
     if (!f)
         return FDTD_ERR_IO;
     CheckpointHeader h{};
-    if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, CKP_MAGIC, 8) != 0 || h.version != 1 ||
+    if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, CKP_MAGIC, 8) != 0 || h.version != ckp_version(s) ||
         h.nx != s->nx || h.ny != s->ny || h.nz != s->nz || h.scheme != s->scheme || h.nclasses != s->nclasses ||
         h.material_hash != s->material_hash || h.steps < 0) {
         std::fclose(f);
@@ -389,7 +395,7 @@ int fdtd_solver_restore(fdtd_solver *s, const char *path)
     state_arrays(s, h.steps, arrs);
     std::vector<float> buf(s->ncell);
     bool ok = true;
-    for (int k = 0; k < 15 && ok && st == FDTD_OK; k++) {
+    for (int k = 0; k < ckp_arrays(s) && ok && st == FDTD_OK; k++) {
         ok = std::fread(buf.data(), sizeof(float), s->ncell, f) == s->ncell;
         if (ok)
             st = cu(cudaMemcpy(arrs[k], buf.data(), sizeof(float) * s->ncell, cudaMemcpyHostToDevice));
@@ -401,7 +407,7 @@ int fdtd_solver_restore(fdtd_solver *s, const char *path)
         return FDTD_ERR_FORMAT;
     // with a double-buffered H the other buffer must hold what the step that
     // produced the saved H read (zero where H is never updated); copy it too
-    if (s->kernel == FDTD_KERNEL_SINGLE_PASS)
+    if (s->kernel != FDTD_KERNEL_TWO_PASS)
         for (int c = 0; c < 3 && st == FDTD_OK; c++)
             st = cu(cudaMemcpy(s->h[(h.steps + 1) & 1][c], arrs[c], sizeof(float) * s->ncell,
                                cudaMemcpyDeviceToDevice));

@@ -61,6 +61,9 @@ int launch_de(const NativeConsts &c, cudaStream_t s);
 int launch_mur(const NativeConsts &c, cudaStream_t s);
 // Single-pass step: H, D, sources and E in one z-marching kernel, then Mur.
 int launch_step(const NativeConsts &c, cudaStream_t s);
+// Compact nine-field step (d_cur == d_prev == R, updated in place) + Mur.
+int launch_step_compact(const NativeConsts &c, cudaStream_t s);
+int launch_h_e_compact(const NativeConsts &c, cudaStream_t s);
 
 // The kernels of one step in launch order, each launchable on its own (for
 // per-kernel event timing).

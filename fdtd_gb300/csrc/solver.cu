@@ -26,8 +26,10 @@ fdtd_native_fields step_fields(const fdtd_solver *s, int n)
 {
     fdtd_native_fields f{};
     const int cur = (n + 1) & 1, prv = n & 1;
-    const int hin = s->kernel == FDTD_KERNEL_SINGLE_PASS ? (n & 1) : 0;
-    const int hout = s->kernel == FDTD_KERNEL_SINGLE_PASS ? ((n + 1) & 1) : 0;
+    // single-pass kernels read H from one buffer and write the other
+    const bool hdb = s->kernel != FDTD_KERNEL_TWO_PASS;
+    const int hin = hdb ? (n & 1) : 0;
+    const int hout = hdb ? ((n + 1) & 1) : 0;
     for (int k = 0; k < 3; k++) {
         (&f.hx)[k] = s->h[hin][k];
         (&f.hx_out)[k] = s->h[hout][k];
@@ -45,9 +47,11 @@ const float *field_buffer(const fdtd_solver *s, int field, int count)
 {
     const int comp = field % 3;
     if (field < 3) {
-        const int idx = s->kernel == FDTD_KERNEL_SINGLE_PASS ? (count & 1) : 0;
+        const int idx = s->kernel != FDTD_KERNEL_TWO_PASS ? (count & 1) : 0;
         return s->h[idx][comp];
     }
+    if (field < 6 && s->kernel == FDTD_KERNEL_COMPACT)
+        return nullptr;  // D is not stored
     // E^{count}, D^{count} live in slot (count - 1) % 2; before any step both slots are zero.
     const int slot = count > 0 ? ((count - 1) & 1) : 0;
     return field < 6 ? s->d[slot][comp] : s->e[slot][comp];
@@ -74,6 +78,8 @@ int enqueue_step(fdtd_solver *s, int n)
     int st;
     if (s->kernel == FDTD_KERNEL_SINGLE_PASS) {
         st = launch_step(c, s->stream);
+    } else if (s->kernel == FDTD_KERNEL_COMPACT) {
+        st = launch_step_compact(c, s->stream);
     } else {
         st = launch_h(c, s->stream);
         if (st == FDTD_OK)
@@ -275,7 +281,8 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
 {
     if (!cfg || !out || !cfg->params || !cfg->material || !cfg->specs)
         return FDTD_ERR_INVALID;
-    if (cfg->kernel != FDTD_KERNEL_SINGLE_PASS && cfg->kernel != FDTD_KERNEL_TWO_PASS)
+    if (cfg->kernel != FDTD_KERNEL_SINGLE_PASS && cfg->kernel != FDTD_KERNEL_TWO_PASS &&
+        cfg->kernel != FDTD_KERNEL_COMPACT)
         return FDTD_ERR_INVALID;
     const FdtdParams *p = cfg->params;
     int st = cu(cudaSetDevice(cfg->device));
@@ -310,9 +317,12 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         delete s;
         return st;
     }
-    const int nh = cfg->kernel == FDTD_KERNEL_SINGLE_PASS ? 2 : 1;
+    // H: two buffers for the single-pass kernels, one for the two-pass pair;
+    // E: two slots; D: two slots, or one R array for the compact form
+    const int nh = cfg->kernel == FDTD_KERNEL_TWO_PASS ? 1 : 2;
+    const int nd = cfg->kernel == FDTD_KERNEL_COMPACT ? 1 : 2;
     const size_t fbytes = ((n * sizeof(float)) + 255) & ~size_t(255);
-    const size_t total = fbytes * (3 * nh + 12) + ((n + 255) & ~size_t(255)) + 256;
+    const size_t total = fbytes * (3 * nh + 6 + 3 * nd) + ((n + 255) & ~size_t(255)) + 256;
     st = cu(cudaMalloc(&s->d_block, total));
     if (st == FDTD_OK) {
         char *q = s->d_block;
@@ -325,9 +335,12 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         for (int b = 0; b < 2; b++)
             for (int k = 0; k < 3; k++, q += fbytes)
                 s->e[b][k] = reinterpret_cast<float *>(q);
-        for (int b = 0; b < 2; b++)
+        for (int b = 0; b < nd; b++)
             for (int k = 0; k < 3; k++, q += fbytes)
                 s->d[b][k] = reinterpret_cast<float *>(q);
+        if (nd == 1)
+            for (int k = 0; k < 3; k++)
+                s->d[1][k] = s->d[0][k];
         s->mat = reinterpret_cast<uint8_t *>(q);
         q += (n + 255) & ~size_t(255);
         s->counter = reinterpret_cast<int *>(q);
@@ -432,10 +445,12 @@ int fdtd_solver_get_field(fdtd_solver *s, int field, float *host_out)
 {
     if (!s || !host_out || field < 0 || field >= FDTD_FIELD_COUNT)
         return FDTD_ERR_INVALID;
+    const float *src = field_buffer(s, field, s->steps);
+    if (!src)
+        return FDTD_ERR_INVALID;
     int st = fdtd_solver_synchronize(s);
     if (st == FDTD_OK)
-        st = cu(cudaMemcpy(host_out, field_buffer(s, field, s->steps), sizeof(float) * s->ncell,
-                           cudaMemcpyDeviceToHost));
+        st = cu(cudaMemcpy(host_out, src, sizeof(float) * s->ncell, cudaMemcpyDeviceToHost));
     return st;
 }
 
@@ -460,6 +475,8 @@ int fdtd_solver_set_snapshots(fdtd_solver *s, const fdtd_snapshot_spec *spec)
         return FDTD_ERR_INVALID;
     if (!sp.callback && !sp.output_dir)
         return FDTD_ERR_INVALID;
+    if (s->kernel == FDTD_KERNEL_COMPACT && (sp.field_mask & (7u << FDTD_FIELD_DX)))
+        return FDTD_ERR_INVALID;  // D is not stored
     for (int f = 0; f < FDTD_FIELD_COUNT; f++)
         if (sp.field_mask & (1u << f))
             s->snap_fields.push_back(f);

@@ -26,16 +26,17 @@
 #include <mutex>
 
 #include "native.cuh"
+#include "tma_util.cuh"
 
 namespace fdtd {
 namespace {
 
-constexpr int FTX = 32;            // tile width in x (one warp)
-constexpr int MBAR_SPIN_LIMIT = 1 << 22;
+using namespace tma;
 
-__host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) & ~127; }
 
-template <int TY>
+// Shared-memory layout of one stage for NT tile arrays (9: D^n, D^{n-1},
+// E^{n-1} of the D form; 3: R of the compact form).
+template <int TY, int NT = 9>
 struct Geo {
     static constexpr int EW = FTX + 8, EH = TY + 2;   // E^n box: x0-4 .. x0+TX+3, y0-1 .. y0+TY
     static constexpr int HW = FTX + 4, HH = TY + 1;   // H box: x0-4 .. x0+TX-1, y0-1 .. y0+TY-1
@@ -43,12 +44,12 @@ struct Geo {
     static constexpr int OFF_E = 0;
     static constexpr int OFF_H = OFF_E + 3 * pad128(E_BYTES);
     static constexpr int OFF_T = OFF_H + 3 * pad128(H_BYTES);
-    static constexpr int OFF_M = OFF_T + 9 * pad128(T_BYTES);
+    static constexpr int OFF_M = OFF_T + NT * pad128(T_BYTES);
     static constexpr int STAGE = pad128(OFF_M + M_BYTES);
     static constexpr int HNW = FTX + 1, HNH = TY + 1;  // H^{n+1/2} plane incl. low halo
     static constexpr int HN_BYTES = pad128(3 * HNW * HNH * 4);
     // expected transaction bytes per plane kind
-    static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 9u * T_BYTES + M_BYTES;
+    static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + unsigned(NT) * T_BYTES + M_BYTES;
     static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
     static constexpr unsigned TX_EPI = 3u * E_BYTES;
 };
@@ -58,77 +59,12 @@ struct FusedArgs {
     int zchunk;
 };
 
-// ---------------------------------------------------------------- PTX helpers
-
-__device__ __forceinline__ uint32_t smem_addr(const void *p)
-{
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait: false after MBAR_SPIN_LIMIT polls.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    for (int i = 0; i < MBAR_SPIN_LIMIT; i++)
-        if (mbar_try_wait(bar, parity))
-            return true;
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
-        ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, bool valid)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(valid ? 4 : 0) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-// ------------------------------------------------------------ plane staging
-
-enum PlaneKind { PLANE_FULL = 0, PLANE_PRO = 1, PLANE_EPI = 2 };
-
-template <int TY>
-__device__ __forceinline__ int plane_kind(int z, int zc0, int zc1)
-{
-    return z < zc0 ? PLANE_PRO : (z >= zc1 ? PLANE_EPI : PLANE_FULL);
-}
-
 // TMA: one thread arms the stage's barrier and issues the plane's boxes.
-template <int TY>
+template <int TY, int NT = 9>
 __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
                                 int z)
 {
-    using G = Geo<TY>;
+    using G = Geo<TY, NT>;
     const unsigned bytes = kind == PLANE_FULL ? G::TX_FULL : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI);
     mbar_expect_tx(bar, bytes);
     for (int c = 0; c < 3; c++)
@@ -139,23 +75,23 @@ __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uin
         tma_load_3d(smem_addr(stage + G::OFF_H + c * pad128(G::H_BYTES)), &maps.m[3 + c], x0 - 4, y0 - 1, z, bar);
     if (kind == PLANE_PRO)
         return;
-    for (int k = 0; k < 9; k++)
+    for (int k = 0; k < NT; k++)
         tma_load_3d(smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), &maps.m[6 + k], x0, y0, z, bar);
-    tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[15], x0, y0, z, bar);
+    tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[6 + NT], x0, y0, z, bar);
 }
 
 // Generic: every thread copies part of each box with 4-byte cp.async
 // (zero-filled outside the grid); the material classes are read separately.
-template <int TY>
+template <int TY, int NT = 9>
 __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage, int kind, int x0, int y0, int z,
                                     int tid)
 {
-    using G = Geo<TY>;
-    constexpr int NT = FTX * TY;
+    using G = Geo<TY, NT>;
+    constexpr int NTH = FTX * TY;
     const int nx = c.nx, ny = c.ny, pitch = c.pitch;
     const size_t plane = (size_t)pitch * ny;
     auto box = [&](const float *base, uint32_t dst, int xs, int ys, int w, int h) {
-        for (int i = tid; i < w * h; i += NT) {
+        for (int i = tid; i < w * h; i += NTH) {
             const int gx = xs + i % w, gy = ys + i / w;
             const bool ok = gx >= 0 && gx < nx && gy >= 0 && gy < ny;
             const float *src = ok ? base + (size_t)z * plane + (size_t)gy * pitch + gx : base;
@@ -172,7 +108,7 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
         return;
     const float *tiles[9] = {c.d_cur[0], c.d_cur[1], c.d_cur[2], c.d_prev[0], c.d_prev[1],
                              c.d_prev[2], c.e_prev[0], c.e_prev[1], c.e_prev[2]};
-    for (int k = 0; k < 9; k++)
+    for (int k = 0; k < NT; k++)
         box(tiles[k], smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), x0, y0, FTX, TY);
 }
 
@@ -182,12 +118,13 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
 // stage ring and its barriers continue from earlier units of the same CTA:
 // g0 counts the planes this CTA has staged before.  Returns false when a
 // bounded wait gave up (the error flag is set; the CTA must stop).
-template <int TY, int S, bool TMA>
+template <int TY, int S, bool TMA, bool COMPACT = false>
 __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMaps &maps, int zchunk, int bx, int by,
                                            int bz, unsigned char *smem, const DebyeCoef *coef, uint64_t *bars,
                                            unsigned g0)
 {
-    using G = Geo<TY>;
+    constexpr int NT = COMPACT ? 3 : 9;
+    using G = Geo<TY, NT>;
     const int nx = c.nx, ny = c.ny, nz = c.nz;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FTX + tx;
     const int x0 = bx * FTX, y0 = by * TY;
@@ -207,9 +144,9 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             const int z = p0 + k;
             if (TMA) {
                 if (tid == 0)
-                    issue_plane_tma<TY>(maps, stage(k), bar(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z);
+                    issue_plane_tma<TY, NT>(maps, stage(k), bar(k), plane_kind(z, zc0, zc1), x0, y0, z);
             } else {
-                issue_plane_generic<TY>(c, stage(k), plane_kind<TY>(z, zc0, zc1), x0, y0, z, tid);
+                issue_plane_generic<TY, NT>(c, stage(k), plane_kind(z, zc0, zc1), x0, y0, z, tid);
             }
         }
         if (!TMA)
@@ -322,6 +259,68 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             }
             __syncthreads();
 
+            if constexpr (COMPACT) {
+            if (in_dom) {
+                const size_t i = (size_t)z * plane + col;
+                const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
+                const int t = ty * FTX + tx;
+                const float r0 = T[0 * TS + t], r1 = T[1 * TS + t], r2 = T[2 * TS + t];
+                uint8_t cls;
+                if (TMA) {
+                    cls = (stage(k) + G::OFF_M)[t];
+                } else {
+                    cls = mat_next;
+                    if (z + 1 < zc1)
+                        mat_next = c.mat[i + plane];
+                }
+                if (x >= 1 && x < nx - 1 && y < ny - 1 && zlo)
+                    c.h_out[0][i] = hxn;
+                if (x < nx - 1 && y >= 1 && y < ny - 1 && zlo)
+                    c.h_out[1][i] = hyn;
+                if (x < nx - 1 && y < ny - 1 && zmid)
+                    c.h_out[2][i] = hzn;
+
+                // ---- this step's D increment dD = dt curl H^{n+1/2} (and the sources)
+                const bool xi = x >= 1 && x < nx - 1, yi = y >= 1 && y < ny - 1;
+                const bool dx_on = x < nx - 1 && yi && zmid;
+                const bool dy_on = xi && y < ny - 1 && zmid;
+                const bool dz_on = xi && yi && zlo;
+                float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
+                if (dx_on)
+                    g0 = tcy * (hzn - hnr(2, ty, tx + 1)) - tcz * (hyn - hym);
+                if (dy_on)
+                    g1 = tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
+                bool src = false;
+                for (int s = 0; s < c.nsources; s++)
+                    src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
+                if (dz_on || src) {
+                    g2 = tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
+                    if (src)
+                        g2 = g2 - jz_now;
+                }
+
+                // ---- E^{n+1} = c (d E^n + (2 dt + 2 tau) dD + R^n),  R^{n+1} = -a E^n - 2 tau dD
+                const bool ex_on = x < nx - 1 && yi && zmid;
+                const bool eyz_on = x >= 1 && z >= 1;
+                if (ex_on || eyz_on) {
+                    const DebyeCoef kc = coef[cls];
+                    const float k12 = kc.two_dt + kc.two_tau;
+                    const int r = ty + 1, cc = tx + 4;
+                    if (ex_on) {
+                        const float e = ea(0, r, cc);
+                        c.e_prev[0][i] = kc.c * (kc.d * e + k12 * g0 + r0);
+                        c.d_prev[0][i] = -kc.a * e - kc.two_tau * g0;
+                    }
+                    if (eyz_on) {
+                        const float e1 = ea(1, r, cc), e2 = ea(2, r, cc);
+                        c.e_prev[1][i] = kc.c * (kc.d * e1 + k12 * g1 + r1);
+                        c.d_prev[1][i] = -kc.a * e1 - kc.two_tau * g1;
+                        c.e_prev[2][i] = kc.c * (kc.d * e2 + k12 * g2 + r2);
+                        c.d_prev[2][i] = -kc.a * e2 - kc.two_tau * g2;
+                    }
+                }
+            }
+            } else {
             if (in_dom) {
                 const size_t i = (size_t)z * plane + col;
                 const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
@@ -382,6 +381,7 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     }
                 }
             }
+            }
             hxm = hxn;
             hym = hyn;
         }
@@ -392,12 +392,12 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             if (tid == 0 && kn < nplanes) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const int zn = p0 + kn;
-                issue_plane_tma<TY>(maps, stage(kn), bar(kn), plane_kind<TY>(zn, zc0, zc1), x0, y0, zn);
+                issue_plane_tma<TY, NT>(maps, stage(kn), bar(kn), plane_kind(zn, zc0, zc1), x0, y0, zn);
             }
         } else {
             if (kn < nplanes) {
                 const int zn = p0 + kn;
-                issue_plane_generic<TY>(c, stage(kn), plane_kind<TY>(zn, zc0, zc1), x0, y0, zn, tid);
+                issue_plane_generic<TY, NT>(c, stage(kn), plane_kind(zn, zc0, zc1), x0, y0, zn, tid);
             }
             cp_async_commit();
         }
@@ -409,16 +409,16 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
 
 // Shared-memory layout of a CTA: S stages, the H^{n+1/2} plane, the class
 // table (up to FDTD_MAX_CLASSES entries), S barriers.
-template <int TY, int S>
+template <int TY, int S, int NT = 9>
 __host__ __device__ constexpr int fused_smem_bytes(int nclasses)
 {
-    return 128 + S * Geo<TY>::STAGE + Geo<TY>::HN_BYTES + nclasses * (int)sizeof(DebyeCoef) + S * 8;
+    return 128 + S * Geo<TY, NT>::STAGE + Geo<TY, NT>::HN_BYTES + nclasses * (int)sizeof(DebyeCoef) + S * 8;
 }
 
-template <int TY, int S, bool TMA>
+template <int TY, int S, bool TMA, int NT = 9>
 __device__ __forceinline__ void fused_cta_setup(unsigned char *smem, DebyeCoef **coef, uint64_t **bars)
 {
-    using G = Geo<TY>;
+    using G = Geo<TY, NT>;
     *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
     *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * sizeof(DebyeCoef));
     const int tid = threadIdx.y * FTX + threadIdx.x;
@@ -439,7 +439,7 @@ __device__ __forceinline__ void load_coef(const NativeConsts &c, DebyeCoef *coef
 }
 
 // One solve: CTA (bx, by, bz) processes one unit.
-template <int TY, int S, bool TMA>
+template <int TY, int S, bool TMA, bool COMPACT>
 __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
                                                              const __grid_constant__ FusedMaps maps)
 {
@@ -447,10 +447,10 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
     DebyeCoef *coef;
     uint64_t *bars;
-    fused_cta_setup<TY, S, TMA>(smem, &coef, &bars);
+    fused_cta_setup<TY, S, TMA, COMPACT ? 3 : 9>(smem, &coef, &bars);
     load_coef(a.c, coef, FTX * TY);
     __syncthreads();
-    fused_unit<TY, S, TMA>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, blockIdx.z, smem, coef, bars, 0u);
+    fused_unit<TY, S, TMA, COMPACT>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, blockIdx.z, smem, coef, bars, 0u);
 }
 
 // Many solves: persistent CTAs take work units from a counter; a unit's solve
@@ -554,50 +554,14 @@ __global__ void batch_advance_kernel(const BatchDesc *__restrict__ descs, int ns
 constexpr int TY_SEL = 8;
 constexpr int S_SEL = 3;
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    });
-    return fn;
-}
 
-bool encode_map(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void *base, bool is_u8, int nx, int ny,
-                int nz, int pitch, int bx, int by)
-{
-    const size_t es = is_u8 ? 1 : 4;
-    cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-    cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)((size_t)pitch * ny * es)};
-    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
-    cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r =
-        fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base),
-           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
-
-bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
-
-template <bool TMA>
+template <bool TMA, bool COMPACT>
 int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
-    using G = Geo<TY_SEL>;
-    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA>;
-    const int smem = fused_smem_bytes<TY_SEL, S_SEL>(FDTD_MAX_CLASSES);
+    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA, COMPACT>;
+    const int smem = fused_smem_bytes<TY_SEL, S_SEL, COMPACT ? 3 : 9>(FDTD_MAX_CLASSES);
     static std::once_flag once;
-    std::call_once(once, [&] {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             128 + S_SEL * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * (int)sizeof(DebyeCoef) +
-                                 S_SEL * 8);
-    });
+    std::call_once(once, [&] { cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); });
     const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
     kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(a, maps);
     const cudaError_t e = cudaGetLastError();
@@ -625,23 +589,29 @@ bool fused_uses_tma(const NativeConsts &c)
     return aligned16(c.mat);
 }
 
-bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps)
+// Tensor maps of one step: E^n and H^{n-1/2} halo boxes (0-5), the tile
+// arrays (D form: D^n, D^{n-1}, E^{n-1} at 6-14; compact form: R at 6-8) and
+// the class volume after them.
+bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps)
 {
     memset(maps, 0, sizeof *maps);
     if (!fused_uses_tma(c))
         return false;
     auto fn = encode_fn();
     using G = Geo<TY_SEL>;
+    const float *const *tiles[3] = {c.d_cur, c.d_prev, c.e_prev};
+    const int ntile_sets = compact ? 1 : 3;
     bool ok = true;
     for (int k = 0; k < 3 && ok; k++) {
         ok &= encode_map(fn, &maps->m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, c.pitch, G::EW, G::EH);
         ok &= encode_map(fn, &maps->m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, c.pitch, G::HW, G::HH);
-        ok &= encode_map(fn, &maps->m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
-        ok &= encode_map(fn, &maps->m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
-        ok &= encode_map(fn, &maps->m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+        for (int t = 0; t < ntile_sets; t++)
+            ok &= encode_map(fn, &maps->m[6 + 3 * t + k], tiles[t][k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
     }
-    return ok && encode_map(fn, &maps->m[15], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+    return ok && encode_map(fn, &maps->m[6 + 3 * ntile_sets], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
 }
+
+bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps) { return encode_step_maps(c, false, maps); }
 
 int fused_tile_height() { return TY_SEL; }
 
@@ -688,23 +658,22 @@ int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
     if (a.zchunk < 1)
         a.zchunk = c.nz;
     FusedMaps maps;
-    memset(&maps, 0, sizeof maps);
-    if (fused_uses_tma(c)) {
-        auto fn = encode_fn();
-        using G = Geo<TY_SEL>;
-        bool ok = true;
-        for (int k = 0; k < 3 && ok; k++) {
-            ok &= encode_map(fn, &maps.m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, c.pitch, G::EW, G::EH);
-            ok &= encode_map(fn, &maps.m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, c.pitch, G::HW, G::HH);
-            ok &= encode_map(fn, &maps.m[6 + k], c.d_cur[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
-            ok &= encode_map(fn, &maps.m[9 + k], c.d_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
-            ok &= encode_map(fn, &maps.m[12 + k], c.e_prev[k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
-        }
-        ok &= encode_map(fn, &maps.m[15], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
-        if (ok)
-            return launch_fused_impl<true>(a, maps, s);
-    }
-    return launch_fused_impl<false>(a, maps, s);
+    if (encode_step_maps(c, false, &maps))
+        return launch_fused_impl<true, false>(a, maps, s);
+    return launch_fused_impl<false, false>(a, maps, s);
+}
+
+int launch_h_e_compact(const NativeConsts &c, cudaStream_t s)
+{
+    if (c.d_cur[0] != c.d_prev[0] || c.d_cur[1] != c.d_prev[1] || c.d_cur[2] != c.d_prev[2])
+        return FDTD_ERR_INVALID;  // R is updated in place
+    FusedArgs a;
+    a.c = c;
+    a.zchunk = fused_zchunk(c.nz);
+    FusedMaps maps;
+    if (encode_step_maps(c, true, &maps))
+        return launch_fused_impl<true, true>(a, maps, s);
+    return launch_fused_impl<false, true>(a, maps, s);
 }
 
 int launch_step(const NativeConsts &c, cudaStream_t s)
@@ -715,12 +684,23 @@ int launch_step(const NativeConsts &c, cudaStream_t s)
     return st;
 }
 
+int launch_step_compact(const NativeConsts &c, cudaStream_t s)
+{
+    int st = launch_h_e_compact(c, s);
+    if (st == FDTD_OK)
+        st = launch_mur(c, s);
+    return st;
+}
+
 int step_kernels(int kernel_kind, const NativeConsts &, StepKernel *out, int max)
 {
-    StepKernel single[] = {{"fused_step", launch_h_de_fused}, {"mur", launch_mur}};
-    StepKernel two[] = {{"h", launch_h}, {"de", launch_de}, {"mur", launch_mur}};
-    const StepKernel *src = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? single : two;
-    const int n = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? 2 : 3;
+    static const StepKernel single[] = {{"fused_step", launch_h_de_fused}, {"mur", launch_mur}};
+    static const StepKernel compact[] = {{"compact_step", launch_h_e_compact}, {"mur", launch_mur}};
+    static const StepKernel two[] = {{"h", launch_h}, {"de", launch_de}, {"mur", launch_mur}};
+    const StepKernel *src = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? single
+                            : kernel_kind == FDTD_KERNEL_COMPACT ? compact
+                                                                   : two;
+    const int n = kernel_kind == FDTD_KERNEL_TWO_PASS ? 3 : 2;
     for (int k = 0; k < n && k < max; k++)
         out[k] = src[k];
     return n;

@@ -130,10 +130,13 @@ def ellipsoid_phantom(shape: tuple[int, int, int], n_shells: int = 8, seed: int 
     nz, ny, nx = shape
     rng = np.random.default_rng(seed)
     base = np.linspace(semi_max, semi_min, n_shells)
+    # keep a margin of vacuum to the Mur faces: 24 cells, or 1/8 of a small axis
+    half = np.array([nx, ny, nz], np.float64) / 2
+    room = np.maximum(half - np.minimum(24.0, np.floor(2 * half / 8)), 1.0)
     axes = []
     for b in base:
         a = b * (1.0 + rng.uniform(-jitter, jitter, 3))
-        axes.append(np.minimum(a, [nx / 2 - 24, ny / 2 - 24, nz / 2 - 24]))
+        axes.append(np.maximum(np.minimum(a, room), 1.0))
     cx, cy, cz = (nx - 1) / 2, (ny - 1) / 2, (nz - 1) / 2
     codes = np.zeros(shape, np.uint8)
     xs = ((np.arange(nx) - cx) ** 2)[None, None, :]

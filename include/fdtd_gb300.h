@@ -277,7 +277,15 @@ typedef struct fdtd_solver fdtd_solver;
 
 enum {
     FDTD_KERNEL_SINGLE_PASS = 0,  /* fdtd_step: one z-marching kernel per step */
-    FDTD_KERNEL_TWO_PASS = 1      /* fdtd_step_h + fdtd_step_de */
+    FDTD_KERNEL_TWO_PASS = 1,     /* fdtd_step_h + fdtd_step_de */
+    /* Single pass over nine stored fields instead of fifteen: D and E^{n-1}
+     * are folded into one recursion variable per component,
+     *   R^n = -a E^{n-1} - 2 tau (D^n - D^{n-1}),
+     *   E^{n+1} = c (d E^n + (2 dt + 2 tau)(D^{n+1} - D^n) + R^n),
+     * the same update as updateEField (fdtd_calculations.cu:141-183)
+     * rearranged, 73 instead of 97 bytes of traffic per cell update.  D is not
+     * stored: the D fields cannot be read, snapshotted or probed. */
+    FDTD_KERNEL_COMPACT = 2
 };
 
 /* Field selectors; bit (1 << FDTD_FIELD_x) in snapshot masks. */
