@@ -7,6 +7,12 @@
   loops it over the reference launch grid).
 * ``oracle/_ref/libref_host.so``: the reference's host set-up code (params
   parser, source table, voxeliser, snapshot writer) behind C wrappers.
+* ``oracle/_ref/ref_kernels.cubin``: the reference's kernel file compiled for
+  sm_103a with the reference Makefile's nvcc defaults (device code only, so
+  it runs on any host with a GB300).
+* ``oracle/_build/libref_gpu.so``: our harness that loads that cubin and
+  drives the reference kernels on the GPU (``ref/ref_gpu.cu``); built on every
+  host with nvcc, used only where the cubin exists.
 
 The ``_ref`` libraries are built only where the reference sources exist
 (``FDTD_REFERENCE_ROOT``, default ``/root/reference``); they compile the
@@ -30,6 +36,8 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 ORACLE_LIBS = {"f64": BUILD / "liboracle_f64.so", "f32": BUILD / "liboracle_f32.so"}
 REF_CPU_LIB = REF_OUT / "libref_cpu.so"
 REF_HOST_LIB = REF_OUT / "libref_host.so"
+REF_CUBIN = REF_OUT / "ref_kernels.cubin"
+REF_GPU_LIB = BUILD / "libref_gpu.so"
 
 
 def _run(cmd: list[str]) -> None:
@@ -55,6 +63,11 @@ def build_oracle(force: bool = False) -> dict[str, Path]:
         if force or _stale(out, [src, Path(__file__)]):
             jobs.append(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp",
                          "-ffp-contract=off", f"-DORACLE_REAL={real}", str(src), "-o", str(out), "-lm"])
+    gpu_src = HERE / "ref" / "ref_gpu.cu"
+    nvcc = CUDA_HOME / "bin" / "nvcc"
+    if nvcc.exists() and (force or _stale(REF_GPU_LIB, [gpu_src])):
+        jobs.append([str(nvcc), "-O2", "-shared", "-Xcompiler", "-fPIC", "-gencode", "arch=compute_103a,code=sm_103a",
+                     str(gpu_src), "-o", str(REF_GPU_LIB), f"-L{CUDA_HOME / 'lib64' / 'stubs'}", "-lcuda"])
     with ThreadPoolExecutor(len(jobs) or 1) as ex:
         list(ex.map(_run, jobs))
     return dict(ORACLE_LIBS)
@@ -104,10 +117,17 @@ def build_reference(force: bool = False) -> dict[str, Path] | None:
         _run([nvcc, "-shared", "-o", str(REF_HOST_LIB)] + [str(o) for o in objs])
         shutil.rmtree(tmp, ignore_errors=True)
 
-    with ThreadPoolExecutor(2) as ex:
-        for f in [ex.submit(cpu), ex.submit(host)]:
+    def cubin() -> None:
+        # the reference Makefile's nvcc invocation (no optimisation or
+        # fast-math options) with the GB300 target; device code only
+        if force or _stale(REF_CUBIN, [ref / "fdtd_calculations.cu", ref / "fdtd_calculations.h"]):
+            _run([str(CUDA_HOME / "bin" / "nvcc"), "-cubin", "-w", "-gencode", "arch=compute_103a,code=sm_103a",
+                  f"-I{ref}", str(ref / "fdtd_calculations.cu"), "-o", str(REF_CUBIN)])
+
+    with ThreadPoolExecutor(3) as ex:
+        for f in [ex.submit(cpu), ex.submit(host), ex.submit(cubin)]:
             f.result()
-    return {"cpu": REF_CPU_LIB, "host": REF_HOST_LIB}
+    return {"cpu": REF_CPU_LIB, "host": REF_HOST_LIB, "cubin": REF_CUBIN}
 
 
 def build(force: bool = False) -> None:

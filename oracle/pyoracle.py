@@ -263,3 +263,63 @@ def ref_cpu_run(cfg: OracleCfg, media: Media, state: State, step0: int, nsteps: 
     m = (P * 4)(*[_ptr(a) for a in (media.sigma, media.eps_i, media.eps_s, media.tau_d)])
     rp = (P * 6)(*[_ptr(a) for a in media.rp])
     L.ref_cpu_run(st, m, rp, step0, nsteps)
+
+
+# ------------------------------------------------- reference kernels on GPU
+
+class RefGpuProblem(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("dt", C.c_float), ("dx", C.c_float), ("dy", C.c_float), ("dz", C.c_float),
+        ("mu0", C.c_float), ("eps0", C.c_float),
+        ("nsources", C.c_int), ("sources", C.POINTER(C.c_int)),
+        ("njz", C.c_int), ("jz", C.POINTER(C.c_float)),
+        ("media", C.POINTER(C.c_float) * 4), ("rp", C.POINTER(C.c_float) * 6),
+    ]
+
+
+def ref_gpu_available() -> bool:
+    """True where the reference kernels were compiled to a cubin (built in a
+    container holding the reference sources; the cubin travels with the repo)."""
+    return _build.REF_CUBIN.exists()
+
+
+def _ref_gpu_lib() -> C.CDLL:
+    if "ref_gpu" not in _LIBS:
+        _build.build_oracle()
+        L = C.CDLL(str(_build.REF_GPU_LIB))
+        rc = L.ref_gpu_load(str(_build.REF_CUBIN).encode())
+        if rc != 0:
+            raise RuntimeError(f"ref_gpu_load failed: {rc}")
+        _LIBS["ref_gpu"] = L
+    return _LIBS["ref_gpu"]
+
+
+def ref_gpu_run(cfg: OracleCfg, media: Media, nsteps: int, warmup: int = 0, state: State | None = None) -> float:
+    """Runs the reference's own CUDA kernels (launch grid, slot rotation and
+    step order of fdtd.cu:75-530) for warmup + nsteps steps from zero; fills
+    ``state`` (float32) if given and returns the milliseconds of the nsteps
+    timed steps.  Step indices must stay below 512 (the reference's dJz)."""
+    L = _ref_gpu_lib()
+    src, jz = cfg._keep
+    keep = [np.ascontiguousarray(a, np.float32) for a in (media.sigma, media.eps_i, media.eps_s, media.tau_d)]
+    rps = [np.ascontiguousarray(a, np.float32) for a in media.rp]
+    prob = RefGpuProblem(nx=cfg.nx, ny=cfg.ny, nz=cfg.nz, dt=cfg.dt, dx=cfg.dx, dy=cfg.dy, dz=cfg.dz, mu0=cfg.mu0,
+                         eps0=cfg.eps0, nsources=cfg.nsources, sources=_ptr(src, C.c_int), njz=len(jz), jz=_ptr(jz))
+    for k, a in enumerate(keep):
+        prob.media[k] = _ptr(a)
+    for k, a in enumerate(rps):
+        prob.rp[k] = _ptr(a)
+    n = cfg.nx * cfg.ny * cfg.nz
+    out = None
+    if state is not None:
+        assert state.dtype == np.float32
+        out = np.empty((21, n), np.float32)
+    ms = C.c_float(0.0)
+    rc = L.ref_gpu_run(C.byref(prob), warmup, nsteps, None if out is None else _ptr(out), C.byref(ms))
+    if rc != 0:
+        raise RuntimeError(f"ref_gpu_run failed: {rc}")
+    if state is not None:
+        for a, src_a in zip(state.arrays(), out):
+            a[...] = src_a.reshape(a.shape)
+    return float(ms.value)
