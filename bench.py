@@ -64,6 +64,7 @@ def parse_args():
     ap.add_argument("--scheme", choices=["reference", "corrected"], default="reference")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the compact-form line of the default run")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
     return ap.parse_args()
 
@@ -260,6 +261,38 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
     kernels_per_step = len(prof)
     s.close()
 
+    # ---- the compact nine-field form on the same workload (reported beside
+    # the D form; same metric, same timing rules, its own clock record)
+    forms = {}
+    if args.kernel == "single" and not args.no_forms:
+        c = fg.Solver(p, codes, specs, scheme=scheme, kernel=KERNELS["compact"], device=local_rank)
+        cstream = torch.cuda.ExternalStream(c.stream)
+        c.run(args.warmup)
+        c.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(local_rank) as cclk:
+            replicas.barrier(dist)
+            torch.cuda.synchronize()
+            a.record(cstream)
+            c.run(args.steps)
+            b.record(cstream)
+            c.synchronize()
+            torch.cuda.synchronize()
+            replicas.barrier(dist)
+        c_cells, c_t = replicas.aggregate(cells * args.steps, a.elapsed_time(b) / 1e3, dist,
+                                          device=f"cuda:{local_rank}")
+        cprof = c.profile(min(args.steps, 20))
+        c.close()
+        cmain = max(cprof, key=cprof.get)
+        forms["compact"] = {
+            "value": c_cells / c_t, "unit": "cell-updates/s", "ms_per_step": c_t / args.steps * 1e3,
+            "state": "H (2 buffers), E (2 slots), R = -a E^{n-1} - 2 tau (D^n - D^{n-1}); D not stored",
+            "b_alg_bytes_per_cell_update": FORM_BYTES["compact"], "kernel_ms": cprof,
+            "roofline_kernel": cmain,
+            "roofline_achieved_gbs": KERNEL_BYTES.get(cmain, 0) * cells / (cprof[cmain] / 1e3) / 1e9,
+            "roofline_traffic": committed_traffic(cmain, cells),
+            "gpu_launches": len(cprof) * args.steps, "clocks": cclk.summary()}
+
     # ---- end to end through the C ABI with host buffers (e2e)
     e2e = None
     if not args.no_e2e:
@@ -318,6 +351,10 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
         "e2e": e2e,
         "cpu_baseline": cpu,
     }
+    if forms:
+        for f in forms.values():
+            f["roofline_frac"] = f["roofline_achieved_gbs"] / peak
+        line["forms"] = forms
     print(json.dumps(line), flush=True)
 
 

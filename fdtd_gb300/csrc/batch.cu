@@ -262,6 +262,11 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
     const FdtdParams *p = cfg->params;
     if (p->nx < 3 || p->ny < 3 || p->nz < 3)
         return FDTD_ERR_INVALID;
+    for (int f = 0; f < 12; f++) {  // the Mur block table indexes face cells with 32-bit offsets
+        const MurFace m = mur_face(f, p->nx, p->ny, p->nz);
+        if ((long long)m.len_u * m.len_v >= (1ll << 31))
+            return FDTD_ERR_INVALID;
+    }
     int st = cu(cudaSetDevice(b->device));
     if (st == FDTD_OK)
         st = cu(cudaStreamSynchronize(b->stream));

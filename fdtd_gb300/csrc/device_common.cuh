@@ -55,9 +55,14 @@ __device__ __forceinline__ DebyeCoef cell_coef(float dt, float eps0, float sigma
 __device__ __forceinline__ float mur_value(float dt, float h, float me, float rp_self, float rp_nbr, float t_nbr,
                                            float s_nbr, float s_self)
 {
-    const float q_self = h * sqrtf(me * rp_self);
-    const float q_nbr = h * sqrtf(me * rp_nbr);
-    return 1.0f / (dt + q_self) * ((dt - q_nbr) * t_nbr + (dt + q_nbr) * s_nbr - (dt - q_self) * s_self);
+    // every operation rounded on its own, in the reference's order
+    // (fdtd_calculations.cu:240-247): no contraction into fused multiply-adds,
+    // so each kernel that applies a Mur face gets the same bits
+    const float q_self = __fmul_rn(h, sqrtf(__fmul_rn(me, rp_self)));
+    const float q_nbr = __fmul_rn(h, sqrtf(__fmul_rn(me, rp_nbr)));
+    const float num = __fsub_rn(__fadd_rn(__fmul_rn(__fsub_rn(dt, q_nbr), t_nbr), __fmul_rn(__fadd_rn(dt, q_nbr), s_nbr)),
+                                __fmul_rn(__fsub_rn(dt, q_self), s_self));
+    return __fmul_rn(__fdiv_rn(1.0f, __fadd_rn(dt, q_self)), num);
 }
 
 // The twelve (component, face) sets that updateMurBoundary writes.  For face
@@ -138,6 +143,69 @@ __device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny,
     const bool quirk = m.comp == 1 && m.axis == 0 && m.far && !fix_ey;
     const float t_nbr = quirk ? S[j] : T[j];
     T[i] = mur_value(dt, h, me, rs, rn, t_nbr, S[j], S[i]);
+}
+
+// mur_apply for K cells of one face set at in-face rows iv0, iv0 + vstride,
+// ... below v_end: all loads are issued before any store, so K independent loads per
+// array are in flight per thread (face cells are written, their neighbours
+// and E^n are only read, so no cell is both).
+template <int K>
+__device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride, int v_end, int nx, int ny, int nz,
+                                            int pitch,
+                                            float dt, float hx, float hy, float hz, float me, const MurSlabs &rp,
+                                            float *t0, float *t1, float *t2, const float *s0, const float *s1,
+                                            const float *s2, bool fix_ey)
+{
+    const MurFace m = mur_face(f, nx, ny, nz);
+    if (iu >= m.len_u)
+        return;
+    const int u = m.u0 + iu;
+    const float *S = m.comp == 0 ? s0 : (m.comp == 1 ? s1 : s2);
+    float *T = m.comp == 0 ? t0 : (m.comp == 1 ? t1 : t2);
+    const bool quirk = m.comp == 1 && m.axis == 0 && m.far && !fix_ey;  // fdtd_calculations.cu:323
+    const float *TN = quirk ? S : T;
+    const float h = m.axis == 0 ? hx : (m.axis == 1 ? hy : hz);
+    const float *slab = m.axis == 0 ? (m.far ? rp.rpx_end : rp.rpx0)
+                        : m.axis == 1 ? (m.far ? rp.rpy_end : rp.rpy0)
+                                      : (m.far ? rp.rpz_end : rp.rpz0);
+    const int ks = m.far ? 1 : 0, kn = m.far ? 0 : 1;
+    float rs[K], rn[K], tn[K], sn[K], sf[K];
+    size_t face[K];
+    bool on[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const int iv = iv0 + k * vstride;
+        on[k] = iv < m.len_v && iv < v_end;
+        const int v = m.v0 + (on[k] ? iv : 0);
+        int x, y, z, dxn = 0, dyn = 0, dzn = 0;
+        size_t rs_i, rn_i;
+        if (m.axis == 0) {
+            x = m.far ? nx - 1 : 0; y = u; z = v; dxn = m.far ? -1 : 1;
+            rs_i = ((size_t)z * ny + y) * 2 + ks;
+            rn_i = ((size_t)z * ny + y) * 2 + kn;
+        } else if (m.axis == 1) {
+            x = u; y = m.far ? ny - 1 : 0; z = v; dyn = m.far ? -1 : 1;
+            rs_i = ((size_t)z * 2 + ks) * nx + x;
+            rn_i = ((size_t)z * 2 + kn) * nx + x;
+        } else {
+            x = u; y = v; z = m.far ? nz - 1 : 0; dzn = m.far ? -1 : 1;
+            rs_i = ((size_t)ks * ny + y) * nx + x;
+            rn_i = ((size_t)kn * ny + y) * nx + x;
+        }
+        face[k] = cell_index(x, y, z, pitch, ny);
+        const size_t j = cell_index(x + dxn, y + dyn, z + dzn, pitch, ny);
+        if (on[k]) {
+            rs[k] = slab[rs_i];
+            rn[k] = slab[rn_i];
+            tn[k] = TN[j];
+            sn[k] = S[j];
+            sf[k] = S[face[k]];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        if (on[k])
+            T[face[k]] = mur_value(dt, h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
 }
 
 }  // namespace fdtd

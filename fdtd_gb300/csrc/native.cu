@@ -64,6 +64,7 @@ NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)
     c.jz = p->d_jz;
     c.njz = p->njz;
     c.rp = p->rp;
+    c.mur_x = p->d_mur_x;
     c.step = n;
     c.step_counter = nullptr;
     c.err = p->d_err;
@@ -192,21 +193,35 @@ __global__ void __launch_bounds__(TX *TY) native_de_kernel(NativeConsts c)
     }
 }
 
-// updateMurBoundary over the face cells of the native state; the last block
-// to run cannot be known, so block (0, 0) advances the device step counter
-// (no other block of this launch reads it).
-__global__ void __launch_bounds__(256) native_mur_kernel(NativeConsts c)
+// updateMurBoundary over the face cells of the native state: blockIdx.z is
+// the face set, x runs along its faster in-face axis, y (strided) along the
+// other.  The last block to run cannot be known, so block (0, 0, 0) advances
+// the device step counter (no other block of this launch reads it).
+constexpr int MUR_THREADS = 128;
+constexpr int MUR_ROWS = 4;  // face rows per thread, loads issued together
+
+__global__ void __launch_bounds__(MUR_THREADS) native_mur_kernel(NativeConsts c)
 {
-    const int f = blockIdx.y;
+    // the next step's single-pass kernel may launch now; its CTAs that read
+    // or write what this kernel touches wait for this grid to complete
+    asm volatile("griddepcontrol.launch_dependents;");
+    const int f = blockIdx.z;
     const MurFace m = mur_face(f, c.nx, c.ny, c.nz);
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c.step_counter && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0)
+    if (c.step_counter && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0)
         atomicAdd(c.step_counter, 1);
-    if (idx >= (long long)m.len_u * m.len_v)
+    const int iu = blockIdx.x * MUR_THREADS + threadIdx.x;
+    if (iu >= m.len_u)
         return;
-    mur_apply(f, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz, c.me, c.rp,
-              c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
-              c.scheme == FDTD_SCHEME_CORRECTED);
+    int len_v = m.len_v;
+    if (m.axis == 0 && (mur_x_fused_faces(c) & (m.far ? 2 : 1))) {
+        if (m.comp == 1)
+            return;  // the single-pass kernel updated this ey face
+        len_v = 1;   // ez: only the z = 0 row is left
+    }
+    const bool fix = c.scheme == FDTD_SCHEME_CORRECTED;
+    for (int iv = blockIdx.y; iv < len_v; iv += MUR_ROWS * gridDim.y)
+        mur_apply_k<MUR_ROWS>(f, iu, iv, gridDim.y, len_v, c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz, c.me, c.rp,
+                              c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2], fix);
 }
 
 int launch_status()
@@ -244,12 +259,15 @@ int launch_de(const NativeConsts &c, cudaStream_t s)
 
 int launch_mur(const NativeConsts &c, cudaStream_t s)
 {
-    long long most = 0;
+    int most_u = 1, most_v = 1;
     for (int f = 0; f < 12; f++) {
         const MurFace m = mur_face(f, c.nx, c.ny, c.nz);
-        most = std::max(most, (long long)m.len_u * m.len_v);
+        most_u = std::max(most_u, m.len_u);
+        most_v = std::max(most_v, m.len_v);
     }
-    native_mur_kernel<<<dim3((unsigned)((most + 255) / 256), 12), 256, 0, s>>>(c);
+    const int rows = (most_v + MUR_ROWS - 1) / MUR_ROWS;
+    const dim3 grid((unsigned)((most_u + MUR_THREADS - 1) / MUR_THREADS), (unsigned)std::min(rows, 65535), 12);
+    native_mur_kernel<<<grid, MUR_THREADS, 0, s>>>(c);
     return launch_status();
 }
 
@@ -350,6 +368,9 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
         offs[2 + k] = cur;
         cur += (sizeof(float) * nrp[k] + 255) & ~size_t(255);
     }
+    const size_t murx_off = cur;
+    const size_t nmurx = 2 * (size_t)p->nz * p->ny;
+    cur += (sizeof(float4) * nmurx + 255) & ~size_t(255);
     const size_t err_off = cur;
     total = cur + 256;
     char *base = nullptr;
@@ -366,7 +387,33 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
         rpd[k] = reinterpret_cast<float *>(base + offs[2 + k]);
     plan->rp = MurSlabs{rpd[0], rpd[1], rpd[2], rpd[3], rpd[4], rpd[5]};
     plan->d_err = reinterpret_cast<int *>(base + err_off);
-    e = cudaMemset(plan->d_err, 0, sizeof(int));
+    plan->d_mur_x = reinterpret_cast<float4 *>(base + murx_off);
+    {
+        // The x-face Mur factors of mur_value, rounded one operation at a time
+        // in the same order (IEEE single: sqrt and division correctly rounded,
+        // no contraction), so the kernel that applies them gets the bits the
+        // Mur kernel gets from the slabs.
+        std::vector<float4> murx(nmurx);
+        const float me = p->mu0 * p->eps0, dt = p->dt, h = p->dx;
+        for (int face = 0; face < 2; face++) {
+            const float *slab = rp[face ? 3 : 0].data();
+            for (int z = 0; z < p->nz; z++)
+                for (int y = 0; y < p->ny; y++) {
+                    const size_t b = ((size_t)z * p->ny + y) * 2;
+                    const float r_self = slab[b + (face ? 1 : 0)], r_nbr = slab[b + (face ? 0 : 1)];
+                    const float q_self = h * std::sqrt(me * r_self), q_nbr = h * std::sqrt(me * r_nbr);
+                    float4 v;
+                    v.x = 1.0f / (dt + q_self);
+                    v.y = dt - q_nbr;
+                    v.z = dt + q_nbr;
+                    v.w = dt - q_self;
+                    murx[((size_t)face * p->nz + z) * p->ny + y] = v;
+                }
+        }
+        e = cudaMemcpy(plan->d_mur_x, murx.data(), sizeof(float4) * nmurx, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess)
+        e = cudaMemset(plan->d_err, 0, sizeof(int));
     if (e == cudaSuccess)
         e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)

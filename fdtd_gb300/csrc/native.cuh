@@ -21,6 +21,7 @@ struct fdtd_plan {
     fdtd::DebyeCoef *d_coef = nullptr;    // nclasses entries
     float *d_jz = nullptr;                // FDTD_JZ_LEN entries
     fdtd::MurSlabs rp{};                  // six Mur slabs
+    float4 *d_mur_x = nullptr;            // x-face Mur coefficients, [face][z][y] (see mur_x_coef)
     int *d_err = nullptr;                 // device error flag
 };
 
@@ -45,6 +46,11 @@ struct NativeConsts {
     int step;              // step index n when step_counter is null
     int *step_counter;     // device step index (graph replay), may be null
     int *err;              // device error flag (a bounded wait gave up)
+    int overlap_prev;      // single-pass launch may start while the previous step's Mur kernel runs
+                           // (programmatic dependent launch; only where that kernel precedes it)
+    int fuse_mur_x;        // the single-pass kernel applies the x-face Mur updates and the Mur
+                           // kernel of the same step skips them (set for both launches or neither)
+    const float4 *mur_x;   // per x-face cell: 1/(dt+q_self), dt-q_nbr, dt+q_nbr, dt-q_self, [face][z][y]
     const float *h_in[3];
     float *h_out[3];
     const float *e_cur[3];
@@ -55,6 +61,17 @@ struct NativeConsts {
 };
 
 NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n);
+
+// x-face Mur updates done by the single-pass kernel: bit 0 the x = 0 face,
+// bit 1 the x = nx-1 face (only when x = nx-2 lies in the same 32-column
+// tile, so one warp holds both cells).  The Mur kernel skips these, except
+// for the ez row at z = 0, whose x = 1 neighbour the single-pass kernel does
+// not update.
+constexpr int FUSED_TILE_X = 32;
+__host__ __device__ inline int mur_x_fused_faces(const NativeConsts &c)
+{
+    return c.fuse_mur_x && c.mur_x ? (1 | ((c.nx - 1) % FUSED_TILE_X != 0 ? 2 : 0)) : 0;
+}
 
 int launch_h(const NativeConsts &c, cudaStream_t s);
 int launch_de(const NativeConsts &c, cudaStream_t s);

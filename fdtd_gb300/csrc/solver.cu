@@ -75,6 +75,9 @@ int enqueue_step(fdtd_solver *s, int n)
     const fdtd_native_fields f = step_fields(s, n);
     NativeConsts c = make_consts(s->plan, &f, n);
     c.step_counter = s->counter;
+    // in a graph the step's first kernel follows the previous step's Mur
+    // kernel unless a monitor kernel runs between them
+    c.overlap_prev = s->nprobes == 0 && !s->dft_on;
     int st;
     if (s->kernel == FDTD_KERNEL_SINGLE_PASS) {
         st = launch_step(c, s->stream);
@@ -522,6 +525,7 @@ int fdtd_solver_profile(fdtd_solver *s, int nsteps, float *avg_ms, int max_kerne
         const fdtd_native_fields f = step_fields(s, n);
         NativeConsts c = make_consts(s->plan, &f, n);
         c.step_counter = s->counter;
+        c.fuse_mur_x = s->kernel != FDTD_KERNEL_TWO_PASS;  // as launch_step sets it
         cudaEvent_t *e = &ev[(size_t)k * (nk + 1)];
         st = cu(cudaEventRecord(e[0], s->stream));
         for (int j = 0; j < nk && st == FDTD_OK; j++) {

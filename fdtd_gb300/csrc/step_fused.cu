@@ -32,6 +32,7 @@ namespace fdtd {
 namespace {
 
 using namespace tma;
+static_assert(FTX == FUSED_TILE_X, "x-face Mur fusion assumes 32-column tiles");
 
 
 // Shared-memory layout of one stage for NT tile arrays (9: D^n, D^{n-1},
@@ -114,6 +115,18 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
 
 // ---------------------------------------------------------------- the kernel
 
+// Whether the unit's columns x0..x0+31, rows y0..y0+ty-1 and planes
+// zc0..zc1-1 hold a source cell.
+__device__ __forceinline__ bool unit_has_source(const NativeConsts &c, int x0, int y0, int ty, int zc0, int zc1)
+{
+    bool any = false;
+    for (int s = 0; s < c.nsources; s++) {
+        const int sx = c.sources[3 * s], sy = c.sources[3 * s + 1], sz = c.sources[3 * s + 2];
+        any |= sx >= x0 && sx < x0 + FTX && sy >= y0 && sy < y0 + ty && sz >= zc0 && sz < zc1;
+    }
+    return any;
+}
+
 // One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
 // stage ring and its barriers continue from earlier units of the same CTA:
 // g0 counts the planes this CTA has staged before.  Returns false when a
@@ -153,9 +166,10 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             cp_async_commit();
     }
 
-    // source of this step (sample index n - n%3 in the reference scheme)
+    // source of this step (sample index n - n%3 in the reference scheme),
+    // read only by units that hold a source cell
     float jz_now = 0.0f;
-    if (c.nsources > 0) {
+    if (unit_has_source(c, x0, y0, TY, zc0, zc1)) {
         const int n = c.step_counter ? *c.step_counter : c.step;
         const int j = c.scheme == FDTD_SCHEME_CORRECTED ? n : n - n % 3;
         jz_now = (j >= 0 && j < c.njz) ? c.jz[j] : 0.0f;
@@ -165,6 +179,22 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
     const size_t plane = (size_t)c.pitch * ny;  // elements between z planes
     const size_t col = (size_t)y * c.pitch + x;
     const float kx = c.kx, ky = c.ky, kz = c.kz, tcx = c.tx, tcy = c.ty, tcz = c.tz;
+    const int cls_max = c.nclasses - 1;  // the table holds nclasses entries; larger codes read the last
+    // x-face Mur updates (updateMurBoundary ey/ez x faces, fdtd_calculations.cu:280-340)
+    // for the tiles that hold x = 0 or x = nx-1: the face lane takes E^{n+1}
+    // of its x-neighbour from the adjacent lane by a shuffle, E^n from the
+    // staged box and the cell's four Mur factors from a register prefetch.
+    const int mur_bits = mur_x_fused_faces(c);
+    const bool face_cta = ((mur_bits & 1) && x0 == 0) || ((mur_bits & 2) && x0 <= nx - 1 && nx - 1 < x0 + FTX);
+    const bool face_far = x == nx - 1;
+    const bool face_lane = x < nx && y < ny && (((mur_bits & 1) && x == 0) || ((mur_bits & 2) && face_far));
+    const float4 *mur_col = face_lane ? c.mur_x + (size_t)(face_far ? 1 : 0) * nz * ny + y : nullptr;
+    float4 mf = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // factors of the face cell at the current plane
+    auto load_mf = [&](int zz) {
+        if (face_lane && zz >= 1 && zz <= nz - 2)
+            mf = mur_col[(size_t)zz * ny];
+    };
+    load_mf(zc0);
     float hxm = 0.0f, hym = 0.0f;  // H^{n+1/2} of this column at z-1
     uint8_t mat_next = 0;
     if (!TMA && in_dom && zc0 < nz)
@@ -259,6 +289,7 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             }
             __syncthreads();
 
+            float ey_new = 0.0f, ez_new = 0.0f;  // this lane's E^{n+1} y, z (for the x-face lanes)
             if constexpr (COMPACT) {
             if (in_dom) {
                 const size_t i = (size_t)z * plane + col;
@@ -303,7 +334,7 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 const bool ex_on = x < nx - 1 && yi && zmid;
                 const bool eyz_on = x >= 1 && z >= 1;
                 if (ex_on || eyz_on) {
-                    const DebyeCoef kc = coef[cls];
+                    const DebyeCoef kc = coef[min((int)cls, cls_max)];
                     const float k12 = kc.two_dt + kc.two_tau;
                     const int r = ty + 1, cc = tx + 4;
                     if (ex_on) {
@@ -313,9 +344,11 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     }
                     if (eyz_on) {
                         const float e1 = ea(1, r, cc), e2 = ea(2, r, cc);
-                        c.e_prev[1][i] = kc.c * (kc.d * e1 + k12 * g1 + r1);
+                        ey_new = kc.c * (kc.d * e1 + k12 * g1 + r1);
+                        ez_new = kc.c * (kc.d * e2 + k12 * g2 + r2);
+                        c.e_prev[1][i] = ey_new;
                         c.d_prev[1][i] = -kc.a * e1 - kc.two_tau * g1;
-                        c.e_prev[2][i] = kc.c * (kc.d * e2 + k12 * g2 + r2);
+                        c.e_prev[2][i] = ez_new;
                         c.d_prev[2][i] = -kc.a * e2 - kc.two_tau * g2;
                     }
                 }
@@ -371,16 +404,40 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 const bool ex_on = x < nx - 1 && yi && zmid;
                 const bool eyz_on = x >= 1 && z >= 1;
                 if (ex_on || eyz_on) {
-                    const DebyeCoef kc = coef[cls];
+                    const DebyeCoef kc = coef[min((int)cls, cls_max)];
                     const int r = ty + 1, cc = tx + 4;
                     if (ex_on)
                         c.e_prev[0][i] = debye_update(kc, ea(0, r, cc), ep0, d0, dn0, dp0);
                     if (eyz_on) {
-                        c.e_prev[1][i] = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
-                        c.e_prev[2][i] = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
+                        ey_new = debye_update(kc, ea(1, r, cc), ep1, d1, dn1, dp1);
+                        ez_new = debye_update(kc, ea(2, r, cc), ep2, d2, dn2, dp2);
+                        c.e_prev[1][i] = ey_new;
+                        c.e_prev[2][i] = ez_new;
                     }
                 }
             }
+            }
+            if (face_cta) {  // uniform over the CTA: every lane takes part in the shuffles
+                const unsigned all = 0xffffffffu;
+                const float ey_hi = __shfl_down_sync(all, ey_new, 1), ez_hi = __shfl_down_sync(all, ez_new, 1);
+                const float ey_lo = __shfl_up_sync(all, ey_new, 1), ez_lo = __shfl_up_sync(all, ez_new, 1);
+                if (face_lane && zmid) {
+                    const size_t i = (size_t)z * plane + col;
+                    const int r = ty + 1, cc = tx + 4, cn = face_far ? cc - 1 : cc + 1;
+                    // mur_value with the factors precomputed, same roundings
+                    auto mur = [&](float tn, float sn, float sf) {
+                        return __fmul_rn(mf.x, __fsub_rn(__fadd_rn(__fmul_rn(mf.y, tn), __fmul_rn(mf.z, sn)),
+                                                         __fmul_rn(mf.w, sf)));
+                    };
+                    if (y <= ny - 2) {  // ey faces: y 0..ny-2, z 1..nz-2
+                        // fdtd_calculations.cu:323: the far ey face reads E^n at x-1 in both terms
+                        const float tn = face_far ? (c.scheme == FDTD_SCHEME_CORRECTED ? ey_lo : ea(1, r, cn)) : ey_hi;
+                        c.e_prev[1][i] = mur(tn, ea(1, r, cn), ea(1, r, cc));
+                    }
+                    if (y >= 1 && y <= ny - 2)  // ez faces: y 1..ny-2, z 0..nz-2 (z = 0 in the Mur kernel)
+                        c.e_prev[2][i] = mur(face_far ? ez_lo : ez_hi, ea(2, r, cn), ea(2, r, cc));
+                }
+                load_mf(z + 1);
             }
             hxm = hxn;
             hym = hyn;
@@ -407,20 +464,24 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
     return true;
 }
 
-// Shared-memory layout of a CTA: S stages, the H^{n+1/2} plane, the class
-// table (up to FDTD_MAX_CLASSES entries), S barriers.
+// Shared-memory layout of a CTA: S stages, the H^{n+1/2} plane, S barriers,
+// then the class table (the launch sizes it for the solve's classes, so a
+// small table leaves room for more resident CTAs).
+template <int S>
+__host__ __device__ constexpr int bars_bytes() { return (S * 8 + 15) & ~15; }
+
 template <int TY, int S, int NT = 9>
 __host__ __device__ constexpr int fused_smem_bytes(int nclasses)
 {
-    return 128 + S * Geo<TY, NT>::STAGE + Geo<TY, NT>::HN_BYTES + nclasses * (int)sizeof(DebyeCoef) + S * 8;
+    return 128 + S * Geo<TY, NT>::STAGE + Geo<TY, NT>::HN_BYTES + bars_bytes<S>() + nclasses * (int)sizeof(DebyeCoef);
 }
 
 template <int TY, int S, bool TMA, int NT = 9>
 __device__ __forceinline__ void fused_cta_setup(unsigned char *smem, DebyeCoef **coef, uint64_t **bars)
 {
     using G = Geo<TY, NT>;
-    *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES);
-    *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES + FDTD_MAX_CLASSES * sizeof(DebyeCoef));
+    *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES);
+    *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES + bars_bytes<S>());
     const int tid = threadIdx.y * FTX + threadIdx.x;
     if (TMA && tid == 0) {
         for (int s = 0; s < S; s++)
@@ -449,8 +510,24 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     uint64_t *bars;
     fused_cta_setup<TY, S, TMA, COMPACT ? 3 : 9>(smem, &coef, &bars);
     load_coef(a.c, coef, FTX * TY);
+    const int bz = blockIdx.z;
+    if (a.c.overlap_prev) {
+        // Launched while the previous step's Mur kernel may still run.  That
+        // kernel writes the E face cells and reads E at faces and their
+        // neighbours (indices 0, 1, n-2, n-1 of each axis) in the buffer this
+        // launch overwrites, and it advances the step counter.  A CTA whose
+        // boxes (x0-4 .. x0+35, y0-1 .. y0+TY, planes zc0-1 .. zc1) stay two
+        // cells clear of every face and that holds no source cell touches
+        // none of that; every other CTA waits for the Mur grid to finish.
+        const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * TY;
+        const int zc0 = bz * a.zchunk, zc1 = min(a.c.nz, zc0 + a.zchunk);
+        const bool clear = x0 - 4 >= 2 && x0 + FTX + 3 <= a.c.nx - 3 && y0 - 1 >= 2 && y0 + TY <= a.c.ny - 3 &&
+                           zc0 - 1 >= 2 && zc1 <= a.c.nz - 3 && !unit_has_source(a.c, x0, y0, TY, zc0, zc1);
+        if (!clear)
+            asm volatile("griddepcontrol.wait;" ::: "memory");
+    }
     __syncthreads();
-    fused_unit<TY, S, TMA, COMPACT>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, blockIdx.z, smem, coef, bars, 0u);
+    fused_unit<TY, S, TMA, COMPACT>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, smem, coef, bars, 0u);
 }
 
 // Many solves: persistent CTAs take work units from a counter; a unit's solve
@@ -529,10 +606,11 @@ __global__ void __launch_bounds__(256) batch_mur_kernel(const BatchDesc *__restr
         return;
     const NativeConsts &c = d.c[n & 1];
     const MurFace m = mur_face(b.face, c.nx, c.ny, c.nz);
-    const long long idx = (long long)b.first + threadIdx.x;
-    if (idx >= (long long)m.len_u * m.len_v)
+    const unsigned idx = (unsigned)b.first + threadIdx.x;  // faces of batched solves hold < 2^31 cells
+    if ((long long)idx >= (long long)m.len_u * m.len_v)
         return;
-    mur_apply(b.face, (int)(idx % m.len_u), (int)(idx / m.len_u), c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz,
+    const unsigned lu = (unsigned)m.len_u;
+    mur_apply(b.face, (int)(idx % lu), (int)(idx / lu), c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz,
               c.me, c.rp, c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
               c.scheme == FDTD_SCHEME_CORRECTED);
 }
@@ -551,20 +629,41 @@ __global__ void batch_advance_kernel(const BatchDesc *__restrict__ descs, int ns
 
 // ------------------------------------------------------------------ host side
 
-constexpr int TY_SEL = 8;
-constexpr int S_SEL = 3;
+// Tile rows and ring depth (build-time constants; 8 x 3 measured fastest).
+#ifndef FDTD_TILE_ROWS
+#define FDTD_TILE_ROWS 8
+#endif
+#ifndef FDTD_RING_STAGES
+#define FDTD_RING_STAGES 3
+#endif
+constexpr int TY_SEL = FDTD_TILE_ROWS;
+constexpr int S_SEL = FDTD_RING_STAGES;
 
 
 template <bool TMA, bool COMPACT>
 int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
     auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA, COMPACT>;
-    const int smem = fused_smem_bytes<TY_SEL, S_SEL, COMPACT ? 3 : 9>(FDTD_MAX_CLASSES);
+    constexpr int NT = COMPACT ? 3 : 9;
     static std::once_flag once;
-    std::call_once(once, [&] { cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem); });
-    const dim3 grid((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
-    kernel<<<grid, dim3(FTX, TY_SEL), smem, s>>>(a, maps);
-    const cudaError_t e = cudaGetLastError();
+    std::call_once(once, [&] {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             fused_smem_bytes<TY_SEL, S_SEL, NT>(FDTD_MAX_CLASSES));
+    });
+    if (a.c.nclasses < 1 || a.c.nclasses > FDTD_MAX_CLASSES)
+        return FDTD_ERR_INVALID;
+    const int smem = fused_smem_bytes<TY_SEL, S_SEL, NT>(a.c.nclasses);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
+    cfg.blockDim = dim3(FTX, TY_SEL);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = a.c.overlap_prev ? 1 : 0;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, a, maps);
     return e == cudaSuccess ? FDTD_OK : (int)e;
 }
 
@@ -676,16 +775,20 @@ int launch_h_e_compact(const NativeConsts &c, cudaStream_t s)
     return launch_fused_impl<false, true>(a, maps, s);
 }
 
-int launch_step(const NativeConsts &c, cudaStream_t s)
+int launch_step(const NativeConsts &c0, cudaStream_t s)
 {
+    NativeConsts c = c0;
+    c.fuse_mur_x = 1;
     int st = launch_h_de_fused(c, s);
     if (st == FDTD_OK)
         st = launch_mur(c, s);
     return st;
 }
 
-int launch_step_compact(const NativeConsts &c, cudaStream_t s)
+int launch_step_compact(const NativeConsts &c0, cudaStream_t s)
 {
+    NativeConsts c = c0;
+    c.fuse_mur_x = 1;
     int st = launch_h_e_compact(c, s);
     if (st == FDTD_OK)
         st = launch_mur(c, s);
