@@ -98,9 +98,11 @@ class ServeResult:
 
 def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_every: int = 250,
           scheme: int = SCHEME_CORRECTED, device: int = 0, clock=time.perf_counter,
-          on_snapshot=None) -> ServeResult:
+          on_snapshot=None, inputs: dict | None = None) -> ServeResult:
     """Runs the request stream to completion in real time.  chunk must
-    divide snapshot_every so snapshots land on exact step counts."""
+    divide snapshot_every so snapshots land on exact step counts.  inputs
+    (optional) maps request ids to build_inputs results that arrive with the
+    requests; missing ones are built at admission."""
     assert snapshot_every % chunk == 0
     pending = sorted(requests, key=lambda r: r.arrival)
     queue: list[Request] = []
@@ -124,7 +126,10 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
                 if batch.bytes + need > budget_bytes:
                     break
                 queue.pop(0)
-                p, codes, specs, src = build_inputs(req, Path(tmp.name) / str(req.rid))
+                if inputs is not None and req.rid in inputs:
+                    p, codes, specs, src = inputs.pop(req.rid)
+                else:
+                    p, codes, specs, src = build_inputs(req, Path(tmp.name) / str(req.rid))
                 sid = batch.add(p, codes, specs, req.steps, scheme=scheme)
                 req.admitted = clock() - t0
                 active[sid] = (req, 0, src[2], p)
