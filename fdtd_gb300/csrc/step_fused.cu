@@ -169,7 +169,21 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
     // source of this step (sample index n - n%3 in the reference scheme),
     // read only by units that hold a source cell
     float jz_now = 0.0f;
-    if (unit_has_source(c, x0, y0, TY, zc0, zc1)) {
+    const bool unit_src = unit_has_source(c, x0, y0, TY, zc0, zc1);
+    // planes p0 + d (d < 66: chunks hold at most 64 planes) at which this
+    // thread's column holds a source: bit d of src_lo, or bit d - 64 of src_hi
+    unsigned long long src_lo = 0ull;
+    unsigned src_hi = 0u;
+    if (unit_src) {
+        for (int s = 0; s < c.nsources; s++) {
+            const int d = c.sources[3 * s + 2] - p0;
+            if (c.sources[3 * s] == x && c.sources[3 * s + 1] == y && d >= 0 && d < 96) {
+                if (d < 64)
+                    src_lo |= 1ull << d;
+                else
+                    src_hi |= 1u << (d - 64);
+            }
+        }
         const int n = c.step_counter ? *c.step_counter : c.step;
         const int j = c.scheme == FDTD_SCHEME_CORRECTED ? n : n - n % 3;
         jz_now = (j >= 0 && j < c.njz) ? c.jz[j] : 0.0f;
@@ -260,19 +274,23 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 hnr(1, ty + 1, tx + 1) = hyn;
                 hnr(2, ty + 1, tx + 1) = hzn;
             }
-            // low-x halo column: hy, hz at x - 1
-            if (tx == 0 && x >= 1 && y < ny) {
-                const int r = ty + 1, cc = 3;  // x - 1
-                const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
-                const int xh = x - 1;
-                float v = ha(1, r, cc);
-                if (y >= 1 && y < ny - 1 && zlo)
-                    v = v - kz * (eb(0, r, cc) - ex_) + kx * (ea(2, r, cc + 1) - ez_);
-                hnr(1, ty + 1, 0) = v;
-                v = ha(2, r, cc);
-                if (xh < nx - 1 && y < ny - 1 && zmid)
-                    v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
-                hnr(2, ty + 1, 0) = v;
+            // low-x halo column: hy, hz at x0 - 1 for the TY rows, one lane of the
+            // last warp per row (the low-y row below is warp 0's)
+            if (ty == TY - 1 && tx < TY) {
+                const int row = tx, yy = y0 + row;
+                if (x0 >= 1 && yy < ny) {
+                    const int r = row + 1, cc = 3;  // x0 - 1
+                    const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
+                    const int xh = x0 - 1;
+                    float v = ha(1, r, cc);
+                    if (yy >= 1 && yy < ny - 1 && zlo)
+                        v = v - kz * (eb(0, r, cc) - ex_) + kx * (ea(2, r, cc + 1) - ez_);
+                    hnr(1, row + 1, 0) = v;
+                    v = ha(2, r, cc);
+                    if (xh < nx - 1 && yy < ny - 1 && zmid)
+                        v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+                    hnr(2, row + 1, 0) = v;
+                }
             }
             // low-y halo row: hx, hz at y - 1
             if (ty == 0 && y >= 1 && x < nx) {
@@ -321,6 +339,8 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     g0 = tcy * (hzn - hnr(2, ty, tx + 1)) - tcz * (hyn - hym);
                 if (dy_on)
                     g1 = tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
+                // the per-cell test over the source list measured faster than the
+                // column mask in this form (5 % on the 512x512x400 phantom)
                 bool src = false;
                 for (int s = 0; s < c.nsources; s++)
                     src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
@@ -387,9 +407,8 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     d0 = dn0 + tcy * (hzn - hnr(2, ty, tx + 1)) - tcz * (hyn - hym);
                 if (dy_on)
                     d1 = dn1 + tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
-                bool src = false;
-                for (int s = 0; s < c.nsources; s++)
-                    src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
+                const int dz = z - p0;
+                const bool src = dz < 64 ? ((src_lo >> dz) & 1ull) : ((src_hi >> (dz - 64)) & 1u);
                 if (dz_on || src) {
                     d2 = dn2 + tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
                     if (src)
@@ -672,7 +691,8 @@ int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 int fused_zchunk(int nz)
 {
     // about 64 planes per CTA: enough CTAs per wave on 152 SMs, little
-    // prologue/epilogue traffic at chunk borders
+    // prologue/epilogue traffic at chunk borders.  At most 64: a unit's
+    // per-thread source mask covers 66 planes.
     const int chunks = (nz + 63) / 64;
     return (nz + chunks - 1) / chunks;
 }
@@ -752,10 +772,7 @@ int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
 {
     FusedArgs a;
     a.c = c;
-    const char *env = getenv("FDTD_ZCHUNK");
-    a.zchunk = env ? atoi(env) : fused_zchunk(c.nz);
-    if (a.zchunk < 1)
-        a.zchunk = c.nz;
+    a.zchunk = fused_zchunk(c.nz);
     FusedMaps maps;
     if (encode_step_maps(c, false, &maps))
         return launch_fused_impl<true, false>(a, maps, s);
