@@ -366,6 +366,9 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
 
 # ------------------------------------------------------- batched / served
 
+def form_name(args) -> str:
+    return "compact form (H, E, R)" if args.kernel == "compact" else "D form"
+
 def _request_inputs(reqs, root: Path, threads: int = 8) -> dict:
     """Inputs of each request (input_params + mat_specs + class volume), built
     in parallel before the clock starts: they arrive with the requests."""
@@ -398,7 +401,7 @@ def run_batch_workload(args) -> None:
                                int(rng.integers(1 << 30))))
     tmp = tempfile.TemporaryDirectory()
     inputs = _request_inputs(reqs, Path(tmp.name))
-    b = fg.Batch(0)
+    b = fg.Batch(0, KERNELS[args.kernel] if args.kernel != "two_pass" else fg.KERNEL_SINGLE_PASS)
     ids = []
     for r in reqs:
         p, codes, specs, src = inputs[r.rid]
@@ -421,17 +424,19 @@ def run_batch_workload(args) -> None:
     cells = [r.dims[0] * r.dims[1] * r.dims[2] for r in reqs]
     updates = sum(c * (r.steps - warm) for c, r in zip(cells, reqs))
     peak, peak_kind = measured_peak_gbs()
+    batch_b = FORM_BYTES["compact" if args.kernel == "compact" else "single"]
     line = {
         "metric": METRIC, "value": updates / seconds, "unit": "cell-updates/s", "n_gpus": 1,
         "steps": longest - warm, "warmup": warm, "ms_per_step": seconds / (longest - warm) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "batch of 64 solves, dims log-uniform 48-256 per axis, 1-4 Debye ellipsoids, "
-                               "source U[0.3,3] GHz, steps U[500,3000], corrected scheme, D form",
+                               f"source U[0.3,3] GHz, steps U[500,3000], corrected scheme, {form_name(args)}",
                    "solves": len(reqs), "cells_total": sum(cells), "state_bytes": b.bytes,
                    "cell_updates": updates, "l2": "state >> 129 MB L2: no flush"},
         "roofline": {"bound": "hbm", "kernel": "batch step (all kernels)",
-                     "achieved": B_ALG * updates / seconds / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": B_ALG * updates / seconds / 1e9 / peak, "peak_kind": peak_kind, "traffic": None},
+                     "achieved": batch_b * updates / seconds / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": batch_b * updates / seconds / 1e9 / peak, "peak_kind": peak_kind, "traffic": None,
+                     "algorithmic_bytes_per_cell_update": batch_b},
         "gpu_launches": 3 * (longest - warm), "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
     }
     b.close()
@@ -453,7 +458,8 @@ def run_serve_workload(args) -> None:
     snaps = []
     with ClockSampler(0) as clk:
         res = sv.serve(reqs, budget_bytes=150 * 10 ** 9, chunk=25, snapshot_every=250, scheme=fg.SCHEME_CORRECTED,
-                       inputs=inputs, on_snapshot=lambda r, step, plane: snaps.append(plane.nbytes))
+                       inputs=inputs, on_snapshot=lambda r, step, plane: snaps.append(plane.nbytes),
+                       kernel=fg.KERNEL_COMPACT if args.kernel == "compact" else fg.KERNEL_SINGLE_PASS)
     summ = res.summary()
     line = {
         "metric": "served cell-updates/s and latency", "value": summ["cell_updates_per_s"],
@@ -461,7 +467,7 @@ def run_serve_workload(args) -> None:
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"Poisson stream {args.serve_rate} req/s for {args.serve_seconds} s, dims "
                                f"log-uniform 64-384, steps U[500,4000], 150 GB budget, Ez snapshot every 250 "
-                               f"steps, corrected scheme, D form", "requests": len(reqs)},
+                               f"steps, corrected scheme, {form_name(args)}", "requests": len(reqs)},
         "serve": {**summ, "snapshot_bytes": int(sum(snaps)), "snapshots": len(snaps)},
         "clocks": clk.summary(),
     }

@@ -156,6 +156,8 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_solver_peak_sar", _I, _V, _P, C.POINTER(C.c_double), C.POINTER(C.c_longlong))
         _sig(L, "fdtd_solver_kernel_name", C.c_char_p, _V, _I)
         _sig(L, "fdtd_batch_create", _I, _I, C.POINTER(_V))
+        _sig(L, "fdtd_batch_create_form", _I, _I, _I, C.POINTER(_V))
+        _sig(L, "fdtd_batch_need_bytes", C.c_size_t, _V, _I, _I, _I)
         _sig(L, "fdtd_batch_destroy", _I, _V)
         _sig(L, "fdtd_batch_solve_bytes", C.c_size_t, _I, _I, _I)
         _sig(L, "fdtd_batch_add", _I, _V, C.POINTER(SolverConfig), _I, C.POINTER(_I))
@@ -419,15 +421,22 @@ class Solver:
 class Batch:
     """Many independent solves advanced together (fdtd_batch_*)."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, kernel: int = KERNEL_SINGLE_PASS):
+        """kernel: KERNEL_SINGLE_PASS (D form) or KERNEL_COMPACT for every solve."""
         h = C.c_void_p()
-        check(lib().fdtd_batch_create(device, C.byref(h)), "fdtd_batch_create")
+        check(lib().fdtd_batch_create_form(device, kernel, C.byref(h)), "fdtd_batch_create_form")
         self.handle = h
+        self.kernel = kernel
         self._keep = {}
 
     @staticmethod
     def solve_bytes(nx: int, ny: int, nz: int) -> int:
+        """Device bytes of one D-form solve."""
         return lib().fdtd_batch_solve_bytes(nx, ny, nz)
+
+    def need_bytes(self, nx: int, ny: int, nz: int) -> int:
+        """Device bytes of one solve of this batch's form."""
+        return lib().fdtd_batch_need_bytes(self.handle, nx, ny, nz)
 
     def add(self, p: Params, material: np.ndarray, specs: np.ndarray, steps: int,
             scheme: int = SCHEME_REFERENCE, nclasses: int | None = None) -> int:
@@ -464,7 +473,8 @@ class Batch:
         return out
 
     def fields(self, sid: int) -> dict[str, np.ndarray]:
-        return {n: self.field(sid, n) for n in FIELDS}
+        names = [n for n in FIELDS if not (self.kernel == KERNEL_COMPACT and n.startswith("d"))]
+        return {n: self.field(sid, n) for n in names}
 
     @property
     def bytes(self) -> int:

@@ -1,6 +1,7 @@
 // batch.cu -- many independent solves of uneven sizes advanced together.
 //
-// Each solve keeps its own resident state (H x2, E x2, D x2, classes) with
+// Each solve keeps its own resident state (H x2, E x2, D x2 or, in a batch of
+// the compact form, R x1, and the classes) with
 // rows padded to a multiple of 16 cells, so every solve gets TMA staging, and
 // its own plan (class table, source table, Mur slabs) and step counter.  A
 // batched step is three launches: one persistent kernel over the work units
@@ -40,17 +41,25 @@ struct BatchSolve {
 
 size_t padded_pitch(int nx) { return ((size_t)nx + 15) & ~size_t(15); }
 
-size_t state_bytes(int nx, int ny, int nz)
+size_t state_bytes(int nx, int ny, int nz, bool compact)
 {
     const size_t ncell = padded_pitch(nx) * ny * nz;
     const size_t f = (ncell * sizeof(float) + 255) & ~size_t(255);
-    return 18 * f + ((ncell + 255) & ~size_t(255)) + 256;
+    return (compact ? 15 : 18) * f + ((ncell + 255) & ~size_t(255)) + 256;
+}
+
+size_t plan_bytes(int nx, int ny, int nz)
+{
+    // class table, source table, Mur slabs, x-face Mur factors
+    return 256 * 32 + 65536 * 4 + 4 * 2 * ((size_t)ny * nz + (size_t)nx * nz + (size_t)nx * ny) +
+           16 * 2 * (size_t)ny * nz + 8 * 256 + 256;
 }
 
 }  // namespace
 
 struct fdtd_batch {
     int device = 0;
+    bool compact = false;  // every solve keeps the compact state
     cudaStream_t stream = nullptr;
     std::vector<BatchSolve *> solves;
     int next_id = 1;
@@ -114,7 +123,7 @@ int rebuild(fdtd_batch *b)
         std::memset(&d, 0, sizeof d);
         for (int par = 0; par < 2; par++) {
             d.c[par] = solve_consts(v, par);
-            if (!encode_fused_maps(d.c[par], &d.maps[par]))
+            if (!encode_step_maps(d.c[par], b->compact, &d.maps[par]))
                 return FDTD_ERR_INVALID;
         }
         d.zchunk = fused_zchunk(v->nz);
@@ -155,8 +164,11 @@ int rebuild(fdtd_batch *b)
         st = cu(cudaStreamSynchronize(b->stream));
     if (st != FDTD_OK)
         return st;
+    int max_classes = 1;
+    for (auto *v : b->solves)
+        max_classes = std::max(max_classes, v->plan->nclasses);
     b->launch = BatchLaunch{b->d_descs, (int)descs.size(), units, b->d_work, b->d_mur, (int)mur.size(),
-                            batch_persistent_ctas()};
+                            batch_persistent_ctas(b->compact, max_classes), b->compact ? 1 : 0, max_classes};
     drop_graphs(b);
     b->dirty = false;
     return FDTD_OK;
@@ -207,14 +219,21 @@ size_t fdtd_batch_solve_bytes(int nx, int ny, int nz)
 {
     if (nx < 3 || ny < 3 || nz < 3)
         return 0;
-    // state + plan (class table, source table, Mur slabs)
-    return state_bytes(nx, ny, nz) + 256 * 32 + 65536 * 4 +
-           4 * 2 * ((size_t)ny * nz + (size_t)nx * nz + (size_t)nx * ny) + 6 * 256 + 256;
+    return state_bytes(nx, ny, nz, false) + plan_bytes(nx, ny, nz);
 }
 
-int fdtd_batch_create(int device, fdtd_batch **out)
+size_t fdtd_batch_need_bytes(const fdtd_batch *b, int nx, int ny, int nz)
 {
-    if (!out)
+    if (!b || nx < 3 || ny < 3 || nz < 3)
+        return 0;
+    return state_bytes(nx, ny, nz, b->compact) + plan_bytes(nx, ny, nz);
+}
+
+int fdtd_batch_create(int device, fdtd_batch **out) { return fdtd_batch_create_form(device, FDTD_KERNEL_SINGLE_PASS, out); }
+
+int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out)
+{
+    if (!out || (kernel != FDTD_KERNEL_SINGLE_PASS && kernel != FDTD_KERNEL_COMPACT))
         return FDTD_ERR_INVALID;
     int st = cu(cudaSetDevice(device));
     if (st != FDTD_OK)
@@ -223,6 +242,7 @@ int fdtd_batch_create(int device, fdtd_batch **out)
     if (!b)
         return FDTD_ERR_NOMEM;
     b->device = device;
+    b->compact = kernel == FDTD_KERNEL_COMPACT;
     st = cu(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     if (st == FDTD_OK)
         st = cu(cudaMalloc(&b->d_work, 256));
@@ -285,7 +305,7 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
     v->steps_target = steps;
     st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &v->plan);
     const size_t fbytes = (v->ncell * sizeof(float) + 255) & ~size_t(255);
-    const size_t total = state_bytes(p->nx, p->ny, p->nz);
+    const size_t total = state_bytes(p->nx, p->ny, p->nz, b->compact);
     if (st == FDTD_OK)
         st = cu(cudaMalloc(&v->d_block, total));
     if (st == FDTD_OK)
@@ -298,9 +318,13 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         for (int s = 0; s < 2; s++)
             for (int k = 0; k < 3; k++, q += fbytes)
                 v->e[s][k] = reinterpret_cast<float *>(q);
-        for (int s = 0; s < 2; s++)
+        const int nd = b->compact ? 1 : 2;  // D^n, D^{n-1} slots, or the one R array
+        for (int s = 0; s < nd; s++)
             for (int k = 0; k < 3; k++, q += fbytes)
                 v->d[s][k] = reinterpret_cast<float *>(q);
+        if (nd == 1)
+            for (int k = 0; k < 3; k++)
+                v->d[1][k] = v->d[0][k];
         v->mat = reinterpret_cast<uint8_t *>(q);
         q += (v->ncell + 255) & ~size_t(255);
         v->counter = reinterpret_cast<int *>(q);
@@ -314,7 +338,7 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         free_solve(v);
         return st;
     }
-    v->bytes = total + fdtd_batch_solve_bytes(p->nx, p->ny, p->nz) - state_bytes(p->nx, p->ny, p->nz);
+    v->bytes = total + plan_bytes(p->nx, p->ny, p->nz);
     v->id = b->next_id++;
     b->solves.push_back(v);
     b->bytes += v->bytes;
@@ -398,6 +422,8 @@ int fdtd_batch_get_field(fdtd_batch *b, int id, int field, int z0, int nplanes, 
     }
     if (z0 < 0 || nplanes < 0 || z0 + nplanes > v->nz)
         return FDTD_ERR_INVALID;
+    if (b->compact && field >= FDTD_FIELD_DX && field <= FDTD_FIELD_DZ)
+        return FDTD_ERR_INVALID;  // D is not stored
     int st = fdtd_batch_synchronize(b);
     int n = 0;
     if (st == FDTD_OK)

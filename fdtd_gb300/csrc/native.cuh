@@ -126,15 +126,18 @@ struct BatchLaunch {
     const BatchMurBlock *mur_blocks;
     int nmur_blocks;
     int persistent_ctas;
+    int compact;      // the batch's solves keep the compact state (d_cur == d_prev == R)
+    int max_classes;  // largest class count of the batch's solves (shared-memory table)
 };
 
 // Tensor maps of a single-pass launch over c's buffers (false: not encodable).
 bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps);
+bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps);
 int fused_tile_height();
 int fused_zchunk(int nz);
 // One batched step: fused kernel over all units, Mur faces, step counters.
 int launch_batch_step(const BatchLaunch &b, cudaStream_t s);
-int batch_persistent_ctas();
+int batch_persistent_ctas(bool compact, int nclasses);
 
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);

@@ -552,8 +552,8 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
 // Many solves: persistent CTAs take work units from a counter; a unit's solve
 // descriptor supplies the constants (copied to shared memory) and tensor maps
 // (read by TMA from device memory).  Units of finished solves are skipped.
-template <int TY, int S>
-__global__ void __launch_bounds__(FTX *TY) batch_step_kernel(const BatchDesc *__restrict__ descs, int nsolves,
+template <int TY, int S, bool COMPACT>
+__global__ void __launch_bounds__(FTX *TY, COMPACT ? 5 : 3) batch_step_kernel(const BatchDesc *__restrict__ descs, int nsolves,
                                                              int total_units, int *work_counter)
 {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -562,7 +562,7 @@ __global__ void __launch_bounds__(FTX *TY) batch_step_kernel(const BatchDesc *__
     __shared__ int s_unit, s_solve;
     DebyeCoef *coef;
     uint64_t *bars;
-    fused_cta_setup<TY, S, true>(smem, &coef, &bars);
+    fused_cta_setup<TY, S, true, COMPACT ? 3 : 9>(smem, &coef, &bars);
     const int tid = threadIdx.y * FTX + threadIdx.x;
     int loaded = -1;
     unsigned g = 0;
@@ -607,7 +607,7 @@ __global__ void __launch_bounds__(FTX *TY) batch_step_kernel(const BatchDesc *__
             const int by = rem / d.tiles_x, bx = rem % d.tiles_x;
             const int zc0 = bz * d.zchunk, zc1 = min(s_c.nz, zc0 + d.zchunk);
             const int nplanes = min(zc1, s_c.nz - 1) - max(zc0 - 1, 0) + 1;
-            if (!fused_unit<TY, S, true>(s_c, d.maps[par], d.zchunk, bx, by, bz, smem, coef, bars, g))
+            if (!fused_unit<TY, S, true, COMPACT>(s_c, d.maps[par], d.zchunk, bx, by, bz, smem, coef, bars, g))
                 return;
             g += (unsigned)nplanes;
         }
@@ -734,28 +734,43 @@ bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps) { return encode_s
 
 int fused_tile_height() { return TY_SEL; }
 
-int batch_persistent_ctas()
+// Shared memory of the persistent batch kernel: tiles of the form and a class
+// table for the batch's largest class count.
+template <bool COMPACT>
+int batch_smem(int nclasses) { return fused_smem_bytes<TY_SEL, S_SEL, COMPACT ? 3 : 9>(nclasses); }
+
+template <bool COMPACT>
+int batch_ctas_impl(int nclasses)
 {
-    static int ctas = 0;
+    auto kernel = batch_step_kernel<TY_SEL, S_SEL, COMPACT>;
     static std::once_flag once;
-    std::call_once(once, [] {
-        auto kernel = batch_step_kernel<TY_SEL, S_SEL>;
-        const int smem = fused_smem_bytes<TY_SEL, S_SEL>(FDTD_MAX_CLASSES);
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FTX * TY_SEL, smem);
-        ctas = sms * (per_sm > 0 ? per_sm : 1);
+    std::call_once(once, [&] {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem<COMPACT>(FDTD_MAX_CLASSES));
     });
-    return ctas;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FTX * TY_SEL, batch_smem<COMPACT>(nclasses));
+    return sms * (per_sm > 0 ? per_sm : 1);
+}
+
+int batch_persistent_ctas(bool compact, int nclasses)
+{
+    return compact ? batch_ctas_impl<true>(nclasses) : batch_ctas_impl<false>(nclasses);
 }
 
 int launch_batch_step(const BatchLaunch &b, cudaStream_t s)
 {
-    const int smem = fused_smem_bytes<TY_SEL, S_SEL>(FDTD_MAX_CLASSES);
-    batch_step_kernel<TY_SEL, S_SEL><<<b.persistent_ctas, dim3(FTX, TY_SEL), smem, s>>>(b.descs, b.nsolves,
-                                                                                         b.total_units, b.work_counter);
+    if (b.max_classes < 1 || b.max_classes > FDTD_MAX_CLASSES)
+        return FDTD_ERR_INVALID;
+    if (b.compact)
+        batch_step_kernel<TY_SEL, S_SEL, true>
+            <<<b.persistent_ctas, dim3(FTX, TY_SEL), batch_smem<true>(b.max_classes), s>>>(
+                b.descs, b.nsolves, b.total_units, b.work_counter);
+    else
+        batch_step_kernel<TY_SEL, S_SEL, false>
+            <<<b.persistent_ctas, dim3(FTX, TY_SEL), batch_smem<false>(b.max_classes), s>>>(
+                b.descs, b.nsolves, b.total_units, b.work_counter);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && b.nmur_blocks > 0) {
         batch_mur_kernel<<<b.nmur_blocks, 256, 0, s>>>(b.descs, b.mur_blocks);

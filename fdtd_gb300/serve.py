@@ -20,7 +20,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import SCHEME_CORRECTED, Batch, Params
+from . import KERNEL_SINGLE_PASS, SCHEME_CORRECTED, Batch, Params
 from . import phantom as ph
 
 
@@ -98,16 +98,17 @@ class ServeResult:
 
 def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_every: int = 250,
           scheme: int = SCHEME_CORRECTED, device: int = 0, clock=time.perf_counter,
-          on_snapshot=None, inputs: dict | None = None) -> ServeResult:
+          on_snapshot=None, inputs: dict | None = None, kernel: int = KERNEL_SINGLE_PASS) -> ServeResult:
     """Runs the request stream to completion in real time.  chunk must
     divide snapshot_every so snapshots land on exact step counts.  inputs
     (optional) maps request ids to build_inputs results that arrive with the
-    requests; missing ones are built at admission."""
+    requests; missing ones are built at admission.  kernel selects the state
+    form of every solve (KERNEL_SINGLE_PASS or KERNEL_COMPACT)."""
     assert snapshot_every % chunk == 0
     pending = sorted(requests, key=lambda r: r.arrival)
     queue: list[Request] = []
     active: dict[int, tuple[Request, int, int, Params]] = {}  # sid -> (req, steps done, snapshot z, params)
-    batch = Batch(device)
+    batch = Batch(device, kernel)
     tmp = tempfile.TemporaryDirectory()
     cell_updates = 0.0
     t0 = clock()
@@ -119,7 +120,7 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
             # admit in arrival order while the head fits the budget
             while queue:
                 req = queue[0]
-                need = Batch.solve_bytes(*req.dims)
+                need = batch.need_bytes(*req.dims)
                 if need > budget_bytes:
                     queue.pop(0)  # can never fit: drop (done stays NaN)
                     continue

@@ -401,12 +401,18 @@ const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k);
 
 typedef struct fdtd_batch fdtd_batch;
 
+/* A batch of the D form (FDTD_KERNEL_SINGLE_PASS state: every field readable). */
 int fdtd_batch_create(int device, fdtd_batch **out);
+/* A batch whose solves all keep the state of `kernel`: FDTD_KERNEL_SINGLE_PASS
+ * (D form) or FDTD_KERNEL_COMPACT (nine fields, D not readable). */
+int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out);
 int fdtd_batch_destroy(fdtd_batch *b);
-/* Device bytes one solve of this grid needs (state + plan), for admission. */
+/* Device bytes one D-form solve of this grid needs (state + plan), for admission. */
 size_t fdtd_batch_solve_bytes(int nx, int ny, int nz);
-/* Adds a solve (cfg->kernel and cfg->device are ignored) that will run
- * `steps` steps; *id receives its handle. */
+/* The same for a solve of this batch's form. */
+size_t fdtd_batch_need_bytes(const fdtd_batch *b, int nx, int ny, int nz);
+/* Adds a solve (cfg->kernel and cfg->device are ignored: the batch's form and
+ * device apply) that will run `steps` steps; *id receives its handle. */
 int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int *id);
 int fdtd_batch_remove(fdtd_batch *b, int id);
 /* Enqueues nsteps batched steps (asynchronous). */

@@ -83,3 +83,28 @@ def test_solves_added_and_removed_while_running(cuda):
 def test_solve_bytes_accounts_state():
     assert fg.Batch.solve_bytes(64, 64, 64) >= 73 * 64 ** 3
     assert fg.Batch.solve_bytes(2, 64, 64) == 0
+
+
+def test_compact_batch_matches_lone_compact_solves_and_oracle(cuda):
+    """A batch of the compact form: every solve equals the compact solver run
+    alone bit for bit and the oracle within the FP32 tolerance (E, H); D is
+    not readable."""
+    b = fg.Batch(kernel=fg.KERNEL_COMPACT)
+    cases = [_case(k) for k in range(len(CASES))]
+    ids = [b.add(Params(c[8]), c[3], c[4], c[1], scheme=c[2]) for c in cases]
+    assert b.need_bytes(64, 64, 64) < fg.Batch.solve_bytes(64, 64, 64)
+    b.run(max(c[1] for c in cases) + 3)
+    for sid, case in zip(ids, cases):
+        dims, steps, scheme, codes, specs, sources, consts, jz, raw = case
+        assert b.steps(sid) == steps
+        got = b.fields(sid)
+        assert sorted(got) == ["ex", "ey", "ez", "hx", "hy", "hz"]
+        with pytest.raises(fg.FdtdError):
+            b.field(sid, "dz")
+        with fg.Solver(Params(raw), codes, specs, scheme=scheme, kernel=fg.KERNEL_COMPACT) as s:
+            s.run(steps)
+            alone = s.fields()
+        for name in got:
+            assert np.array_equal(got[name].view(np.uint32), alone[name].view(np.uint32)), (dims, name)
+        assert_fields_close(got, _oracle(*case), names=list(got))
+    b.close()

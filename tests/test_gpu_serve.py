@@ -23,14 +23,15 @@ class Recorder:
         self.finals[req.rid] = batch.fields(sid)
 
 
-def test_served_results_equal_lone_runs_and_overlap(cuda, tmp_path):
+@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT])
+def test_served_results_equal_lone_runs_and_overlap(cuda, tmp_path, kernel):
     reqs = serve.poisson_stream(rate=40.0, duration=0.3, seed=3, dims=(24, 56), steps=(50, 150))
     assert len(reqs) >= 4
     for r in reqs:  # whole chunks keep the snapshot steps exact
         r.steps = (r.steps // 25) * 25 or 25
     rec = Recorder()
     budget = sum(fg.Batch.solve_bytes(*r.dims) for r in reqs[:3])  # forces queueing
-    res = serve.serve(reqs, budget_bytes=budget, chunk=25, snapshot_every=50, on_snapshot=rec)
+    res = serve.serve(reqs, budget_bytes=budget, chunk=25, snapshot_every=50, on_snapshot=rec, kernel=kernel)
     s = res.summary()
     assert s["completed"] == len(reqs)
     # continuous batching: some request was admitted while another was still running
@@ -39,7 +40,7 @@ def test_served_results_equal_lone_runs_and_overlap(cuda, tmp_path):
     for r in reqs:
         assert r.snapshots[-1] == r.steps
         p, codes, specs, src = serve.build_inputs(r, tmp_path / f"alone{r.rid}")
-        with fg.Solver(p, codes, specs, scheme=fg.SCHEME_CORRECTED) as alone:
+        with fg.Solver(p, codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel) as alone:
             alone.run(r.steps)
             want = alone.fields()
         got = rec.finals[r.rid]
