@@ -14,7 +14,9 @@
 //   --every N            snapshot period in steps (default 1; 0 = no output)
 //   --fields LIST        e.g. ex,ey,ez            (default all nine)
 //   --timeskip X         dt factor                (default 1.0, as the reference)
-//   --kernel single|two  fused single-pass or two-pass kernels
+//   --kernel single|two|compact
+//                        fused single-pass, two-pass, or the single-pass compact
+//                        form (nine stored fields: D is not written)
 //   --device N
 #include <chrono>
 #include <cstdio>
@@ -74,11 +76,16 @@ int main(int argc, char **argv)
         else if (a == "--every") every = std::atoi(next());
         else if (a == "--fields") mask = parse_fields(next());
         else if (a == "--timeskip") timeskip = std::strtof(next(), nullptr);
-        else if (a == "--kernel") kernel = std::strcmp(next(), "two") == 0 ? FDTD_KERNEL_TWO_PASS : FDTD_KERNEL_SINGLE_PASS;
+        else if (a == "--kernel") {
+            const char *k = next();
+            kernel = std::strcmp(k, "two") == 0       ? FDTD_KERNEL_TWO_PASS
+                     : std::strcmp(k, "compact") == 0 ? FDTD_KERNEL_COMPACT
+                                                      : FDTD_KERNEL_SINGLE_PASS;
+        }
         else if (a == "--device") device = std::atoi(next());
         else {
             std::fprintf(stderr, "usage: %s [--params P] [--specs P] [--scheme reference|corrected] [--every N] "
-                                 "[--fields hx,...] [--timeskip X] [--kernel single|two] [--device N]\n", argv[0]);
+                                 "[--fields hx,...] [--timeskip X] [--kernel single|two|compact] [--device N]\n", argv[0]);
             return 2;
         }
     }
@@ -120,6 +127,8 @@ int main(int argc, char **argv)
     fdtd_solver *s = nullptr;
     if ((st = fdtd_solver_create(&cfg, &s)) != FDTD_OK)
         return fail("solver", st);
+    if (kernel == FDTD_KERNEL_COMPACT)
+        mask &= ~(7u << FDTD_FIELD_DX);  // the compact form stores no D
     if (every > 0 && mask) {
         fdtd_snapshot_spec spec{};
         spec.every = every;
