@@ -47,3 +47,28 @@ def test_overlapped_steps_equal_serial_steps_and_oracle(cuda, kernel):
     po.run(po.make_cfg(DIMS, jz, sources=sources, consts=consts, corrected=True), media, st, 0, steps)
     want = st.latest(steps)
     assert_fields_close(runs[True], want, names=[n for n in runs[True]])
+
+
+@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT])
+def test_sources_on_z_chunk_borders(cuda, kernel):
+    """Sources on the planes where z chunks meet: the last plane of a chunk
+    (which the next chunk also stages, to recompute H below its first plane),
+    the first plane of the next chunk, and a pair on the planes either side of
+    a border; against the FP64 oracle."""
+    dims = (70, 26, 150)          # z chunks of 50 planes: [0, 50), [50, 100), [100, 150)
+    steps = 60
+    codes, specs, rp, _, consts, jz = random_case(*dims, seed=5, ncls=3, nsrc=0)
+    sources = [(35, 13, 49), (20, 7, 50), (50, 20, 99), (40, 10, 100), (41, 11, 101)]
+    raw = make_params(dims, consts, sources, jz)
+    with fg.Solver(Params(raw), codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel) as s:
+        s.run(steps)
+        got = s.fields()
+    p = po.OracleParams()
+    p.nx, p.ny, p.nz = dims
+    p.pi, p.wave_frequency, p.eps0 = raw.pi, raw.waveFrequency, raw.eps0
+    p.default_sigma, p.default_eps_s = raw.defaultSigma, raw.defaultEpsS
+    p.default_eps_i, p.default_tau_d = raw.defaultEpsI, raw.defaultTauD
+    media = class_media(codes, specs, po.uniform_media(p).rp)
+    st = po.State(*dims, np.float64)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts, corrected=True), media, st, 0, steps)
+    assert_fields_close(got, st.latest(steps), names=list(got))
