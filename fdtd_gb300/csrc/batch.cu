@@ -292,10 +292,8 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         st = cu(cudaStreamSynchronize(b->stream));
     if (st != FDTD_OK)
         return st;
-    const size_t dense = (size_t)p->nx * p->ny * p->nz;
-    for (size_t i = 0; i < dense; i++)
-        if (cfg->material[i] >= cfg->nclasses)
-            return FDTD_ERR_INVALID;
+    if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, nullptr) != FDTD_OK)
+        return FDTD_ERR_INVALID;
     auto *v = new (std::nothrow) BatchSolve();
     if (!v)
         return FDTD_ERR_NOMEM;

@@ -14,6 +14,7 @@
 
 #include "device_common.cuh"
 #include "native.cuh"
+#include "fdtd_internal.h"
 
 namespace fdtd {
 
@@ -34,6 +35,36 @@ DebyeCoef debye_coef(float dt, float eps0, float sigma, float eps_s, float eps_i
     const float s = dt + tau;
     k.delta = (float)(2.0 * ((double)s - ((double)dt + (double)tau)));
     return k;
+}
+
+int scan_material(const uint8_t *mat, int nx, int ny, int nz, int nclasses, unsigned long long *hash)
+{
+    // per z plane, in parallel: the largest class and an FNV-1a hash; the
+    // plane hashes are then folded in order by FNV-1a over their bytes
+    const size_t plane = (size_t)nx * ny;
+    std::vector<unsigned long long> ph(nz);
+    std::vector<int> top(nz, 0);
+    parallel_for(nz, 0, [&](int z) {
+        const uint8_t *q = mat + (size_t)z * plane;
+        unsigned long long h = 1469598103934665603ULL;
+        int m = 0;
+        for (size_t i = 0; i < plane; i++) {
+            m = q[i] > m ? q[i] : m;
+            h = (h ^ q[i]) * 1099511628211ULL;
+        }
+        ph[z] = h;
+        top[z] = m;
+    });
+    unsigned long long h = 1469598103934665603ULL;
+    for (int z = 0; z < nz; z++) {
+        if (top[z] >= nclasses)
+            return FDTD_ERR_INVALID;
+        for (int b = 0; b < 8; b++)
+            h = (h ^ ((ph[z] >> (8 * b)) & 0xffu)) * 1099511628211ULL;
+    }
+    if (hash)
+        *hash = h;
+    return FDTD_OK;
 }
 
 NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)

@@ -294,9 +294,9 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     const size_t n = (size_t)p->nx * p->ny * p->nz;
     if (p->nx < 3 || p->ny < 3 || p->nz < 3)
         return FDTD_ERR_INVALID;
-    for (size_t i = 0; i < n; i++)
-        if (cfg->material[i] >= cfg->nclasses)
-            return FDTD_ERR_INVALID;
+    unsigned long long mhash = 0;
+    if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, &mhash) != FDTD_OK)
+        return FDTD_ERR_INVALID;
     auto *s = new (std::nothrow) fdtd_solver();
     if (!s)
         return FDTD_ERR_NOMEM;
@@ -307,14 +307,7 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     s->scheme = cfg->scheme;
     s->nclasses = cfg->nclasses;
     s->specs.assign(cfg->specs, cfg->specs + 4 * (size_t)cfg->nclasses);
-    {
-        unsigned long long h = 1469598103934665603ULL;  // FNV-1a of the class volume
-        for (size_t i = 0; i < n; i++) {
-            h ^= cfg->material[i];
-            h *= 1099511628211ULL;
-        }
-        s->material_hash = h;
-    }
+    s->material_hash = mhash;  // checkpoints must come from the same class volume
     st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &s->plan);
     if (st != FDTD_OK) {
         delete s;
