@@ -69,6 +69,9 @@ def parse_args():
     ap.add_argument("--workload", choices=["phantom", "batch", "serve"], default="phantom",
                     help="phantom: the 512x512x400 solve (default); batch: 64 uneven solves in one batch; "
                          "serve: a Poisson request stream through the serving loop")
+    ap.add_argument("--batch-solves", type=int, default=64, help="solves of the batch workload (the first N)")
+    ap.add_argument("--batch-steps", type=int, default=0,
+                    help="timed steps of the batch workload (0: until the last solve ends)")
     ap.add_argument("--serve-rate", type=float, default=2.0, help="requests per second (serve)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the arrival window (serve)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
@@ -399,6 +402,7 @@ def run_batch_workload(args) -> None:
         dims = tuple(int(round(math.exp(rng.uniform(math.log(48), math.log(256))))) for _ in range(3))
         reqs.append(sv.Request(rid, 0.0, dims, float(rng.uniform(3e8, 3e9)), int(rng.integers(500, 3001)),
                                int(rng.integers(1 << 30))))
+    reqs = reqs[:max(1, min(64, args.batch_solves))]
     tmp = tempfile.TemporaryDirectory()
     inputs = _request_inputs(reqs, Path(tmp.name))
     b = fg.Batch(0, KERNELS[args.kernel] if args.kernel != "two_pass" else fg.KERNEL_SINGLE_PASS)
@@ -412,6 +416,8 @@ def run_batch_workload(args) -> None:
     stream = torch.cuda.ExternalStream(b.stream)
     a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     longest = max(r.steps for r in reqs)
+    if args.batch_steps > 0:
+        longest = min(longest, warm + args.batch_steps)
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         a.record(stream)
@@ -420,16 +426,16 @@ def run_batch_workload(args) -> None:
         b.synchronize()
         torch.cuda.synchronize()
     seconds = a.elapsed_time(e) / 1e3
-    assert all(b.steps(i) == r.steps for i, r in zip(ids, reqs))
+    assert all(b.steps(i) == min(r.steps, longest) for i, r in zip(ids, reqs))
     cells = [r.dims[0] * r.dims[1] * r.dims[2] for r in reqs]
-    updates = sum(c * (r.steps - warm) for c, r in zip(cells, reqs))
+    updates = sum(c * (min(r.steps, longest) - warm) for c, r in zip(cells, reqs))
     peak, peak_kind = measured_peak_gbs()
     batch_b = FORM_BYTES["compact" if args.kernel == "compact" else "single"]
     line = {
         "metric": METRIC, "value": updates / seconds, "unit": "cell-updates/s", "n_gpus": 1,
         "steps": longest - warm, "warmup": warm, "ms_per_step": seconds / (longest - warm) * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "batch of 64 solves, dims log-uniform 48-256 per axis, 1-4 Debye ellipsoids, "
+        "config": {"workload": f"batch of {len(reqs)} solves, dims log-uniform 48-256 per axis, 1-4 Debye ellipsoids, "
                                f"source U[0.3,3] GHz, steps U[500,3000], corrected scheme, {form_name(args)}",
                    "solves": len(reqs), "cells_total": sum(cells), "state_bytes": b.bytes,
                    "cell_updates": updates, "l2": "state >> 129 MB L2: no flush"},
