@@ -27,7 +27,7 @@ struct MonitorArgs {
     const float *e[3];         // E after the step
     // probes
     int nprobes, probe_cap, probe_start;
-    const int *probe_idx;
+    const long long *probe_idx;  // cell index of each probe (grids may exceed 2^31 cells)
     float *probe_buf;
     // DFT
     int dft_on, stride;
@@ -44,7 +44,7 @@ __global__ void __launch_bounds__(256) monitor_kernel(MonitorArgs a)
         const int k = m - a.probe_start - 1;
         if (k >= 0 && k < a.probe_cap) {
             const int p = threadIdx.x;
-            const int idx = a.probe_idx[p];
+            const long long idx = a.probe_idx[p];
             float *dst = a.probe_buf + ((size_t)k * a.nprobes + p) * 3;
             dst[0] = a.e[0][idx];
             dst[1] = a.e[1][idx];
@@ -161,12 +161,12 @@ int fdtd_solver_set_probes(fdtd_solver *s, int nprobes, const int *xyz, int capa
 {
     if (!s || nprobes < 0 || nprobes > FDTD_MAX_PROBES || (nprobes > 0 && (!xyz || capacity < 1)))
         return FDTD_ERR_INVALID;
-    std::vector<int> idx(nprobes);
+    std::vector<long long> idx(nprobes);
     for (int p = 0; p < nprobes; p++) {
         const int x = xyz[3 * p], y = xyz[3 * p + 1], z = xyz[3 * p + 2];
         if (x < 0 || x >= s->nx || y < 0 || y >= s->ny || z < 0 || z >= s->nz)
             return FDTD_ERR_INVALID;
-        idx[p] = (int)cell_index(x, y, z, s->nx, s->ny);
+        idx[p] = (long long)cell_index(x, y, z, s->nx, s->ny);
     }
     int st = fdtd_solver_synchronize(s);
     if (st != FDTD_OK)
@@ -179,11 +179,11 @@ int fdtd_solver_set_probes(fdtd_solver *s, int nprobes, const int *xyz, int capa
     reset_graphs(s);
     if (nprobes == 0)
         return FDTD_OK;
-    st = cu(cudaMalloc(&s->d_probe_idx, sizeof(int) * nprobes));
+    st = cu(cudaMalloc(&s->d_probe_idx, sizeof(long long) * nprobes));
     if (st == FDTD_OK)
         st = cu(cudaMalloc(&s->d_probe_buf, sizeof(float) * 3 * (size_t)nprobes * capacity));
     if (st == FDTD_OK)
-        st = cu(cudaMemcpy(s->d_probe_idx, idx.data(), sizeof(int) * nprobes, cudaMemcpyHostToDevice));
+        st = cu(cudaMemcpy(s->d_probe_idx, idx.data(), sizeof(long long) * nprobes, cudaMemcpyHostToDevice));
     if (st == FDTD_OK)
         st = cu(cudaMemset(s->d_probe_buf, 0, sizeof(float) * 3 * (size_t)nprobes * capacity));
     if (st != FDTD_OK)

@@ -62,7 +62,7 @@ struct fdtd_solver {
     std::vector<float> specs;  // nclasses x 4
     // probes
     int nprobes = 0, probe_cap = 0, probe_start = 0;
-    int *d_probe_idx = nullptr;
+    long long *d_probe_idx = nullptr;
     float *d_probe_buf = nullptr;
     // running DFT
     bool dft_on = false;
