@@ -88,7 +88,9 @@ SNAPSHOT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_floa
 class SnapshotSpec(C.Structure):
     _fields_ = [("every", C.c_int), ("field_mask", C.c_uint32), ("z0", C.c_int), ("nplanes", C.c_int),
                 ("callback", SNAPSHOT_FN), ("user", C.c_void_p), ("output_dir", C.c_char_p),
-                ("writer_threads", C.c_int)]
+                ("writer_threads", C.c_int), ("format", C.c_int)]
+
+SNAPSHOT_TEXT, SNAPSHOT_BINARY, SNAPSHOT_TEXT_AND_BINARY = 0, 1, 2
 
 
 _LIB: C.CDLL | None = None
@@ -335,7 +337,11 @@ class Solver:
         return {n: self.field(n) for n in names}
 
     def set_snapshots(self, every: int, fields=("ex", "ey", "ez"), z0: int = 0, nplanes: int = 0,
-                      callback=None, output_dir: str | None = None, writer_threads: int = 0) -> None:
+                      callback=None, output_dir: str | None = None, writer_threads: int = 0,
+                      format: int = SNAPSHOT_TEXT) -> None:
+        """Snapshots every `every` steps to `callback(step, name, planes)`, or to
+        files under output_dir: the reference text layout (SNAPSHOT_TEXT), raw
+        float32 files (SNAPSHOT_BINARY) or both."""
         mask = 0
         for n in fields:
             mask |= 1 << FIELD_ID[n]
@@ -344,7 +350,7 @@ class Solver:
                 step, FIELDS[field], np.ctypeslib.as_array(data, shape=(np_, self.params.ny, self.params.nx)).copy()))
         spec = SnapshotSpec(every=every, field_mask=mask, z0=z0, nplanes=nplanes, callback=cb, user=None,
                             output_dir=None if output_dir is None else str(output_dir).encode(),
-                            writer_threads=writer_threads)
+                            writer_threads=writer_threads, format=format)
         check(lib().fdtd_solver_set_snapshots(self.handle, C.byref(spec)), "fdtd_solver_set_snapshots")
         self._cb, self._spec = cb, spec
 

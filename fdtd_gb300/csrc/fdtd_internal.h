@@ -20,6 +20,9 @@ float mur_rp_value(const FdtdParams *p, float sigma, float eps_s, float eps_i, f
 // Text snapshot helpers (host_io.cpp).
 int write_plane_text(const std::string &path, const float *plane, int nx, int ny);
 std::string snapshot_name(const char *dir, int field, int iteration, int z);
+// Binary snapshot file of nplanes planes from z0, and a raw float writer.
+std::string snapshot_name_f32(const char *dir, int field, int iteration, int z0, int nplanes);
+int write_floats(const std::string &path, const float *data, size_t count);
 
 // cudaGetErrorString for codes below FDTD_ERR_INVALID (cuda_util.cu).
 const char *cuda_error_string(int code);

@@ -13,6 +13,8 @@
 //   --scheme reference|corrected
 //   --every N            snapshot period in steps (default 1; 0 = no output)
 //   --fields LIST        e.g. ex,ey,ez            (default all nine)
+//   --format text|binary|both
+//                        reference text layout (default), raw float32 files, or both
 //   --timeskip X         dt factor                (default 1.0, as the reference)
 //   --kernel single|two|compact
 //                        fused single-pass, two-pass, or the single-pass compact
@@ -59,6 +61,7 @@ int main(int argc, char **argv)
 {
     std::string params_path = "data/input_params", specs_path = "data/mat_specs_riken";
     int scheme = FDTD_SCHEME_REFERENCE, every = 1, device = 0, kernel = FDTD_KERNEL_SINGLE_PASS;
+    int format = FDTD_SNAPSHOT_TEXT;
     uint32_t mask = (1u << FDTD_FIELD_COUNT) - 1;
     float timeskip = 1.0f;
     for (int i = 1; i < argc; i++) {
@@ -75,6 +78,12 @@ int main(int argc, char **argv)
         else if (a == "--scheme") scheme = std::strcmp(next(), "corrected") == 0 ? FDTD_SCHEME_CORRECTED : FDTD_SCHEME_REFERENCE;
         else if (a == "--every") every = std::atoi(next());
         else if (a == "--fields") mask = parse_fields(next());
+        else if (a == "--format") {
+            const char *f = next();
+            format = std::strcmp(f, "binary") == 0 ? FDTD_SNAPSHOT_BINARY
+                     : std::strcmp(f, "both") == 0 ? FDTD_SNAPSHOT_TEXT_AND_BINARY
+                                                   : FDTD_SNAPSHOT_TEXT;
+        }
         else if (a == "--timeskip") timeskip = std::strtof(next(), nullptr);
         else if (a == "--kernel") {
             const char *k = next();
@@ -85,7 +94,7 @@ int main(int argc, char **argv)
         else if (a == "--device") device = std::atoi(next());
         else {
             std::fprintf(stderr, "usage: %s [--params P] [--specs P] [--scheme reference|corrected] [--every N] "
-                                 "[--fields hx,...] [--timeskip X] [--kernel single|two|compact] [--device N]\n", argv[0]);
+                                 "[--fields hx,...] [--format text|binary|both] [--timeskip X] [--kernel single|two|compact] [--device N]\n", argv[0]);
             return 2;
         }
     }
@@ -134,6 +143,7 @@ int main(int argc, char **argv)
         spec.every = every;
         spec.field_mask = mask;
         spec.output_dir = p.outputPath;
+        spec.format = format;
         if ((st = fdtd_solver_set_snapshots(s, &spec)) != FDTD_OK)
             return fail("snapshots", st);
     }

@@ -514,6 +514,27 @@ int write_plane_text(const std::string &path, const float *plane, int nx, int ny
     return (w == out.size() && rc == 0) ? FDTD_OK : FDTD_ERR_IO;
 }
 
+std::string snapshot_name_f32(const char *dir, int field, int iteration, int z0, int nplanes)
+{
+    static const char groups[3] = {'H', 'D', 'E'};
+    static const char comps[3] = {'x', 'y', 'z'};
+    char name[112];
+    std::snprintf(name, sizeof name, "/%c_field_%c_%05d_z%05d_n%05d.f32", groups[field / 3], comps[field % 3],
+                  iteration, z0, nplanes);
+    return std::string(dir) + name;
+}
+
+int write_floats(const std::string &path, const float *data, size_t count)
+{
+    FILE *f = std::fopen(path.c_str(), "wb");
+    if (!f)
+        return FDTD_ERR_IO;
+    // the hosts this builds for (x86-64, aarch64) are little-endian: the bytes
+    // in memory are the file's bytes
+    const bool ok = std::fwrite(data, sizeof(float), count, f) == count;
+    return std::fclose(f) == 0 && ok ? FDTD_OK : FDTD_ERR_IO;
+}
+
 std::string snapshot_name(const char *dir, int field, int iteration, int z)
 {
     static const char groups[3] = {'H', 'D', 'E'};

@@ -194,15 +194,26 @@ void writer_main(fdtd_solver *s)
                 s->snap.callback(s->snap.user, sl.step, s->snap_fields[k], sl.host + k * per, s->snap.z0, np);
         } else {
             const int nf = (int)s->snap_fields.size();
-            std::vector<int> status(nf * np, FDTD_OK);
-            parallel_for(nf * np, s->snap.writer_threads, [&](int j) {
-                const int k = j / np, z = j % np;
-                status[j] = write_plane_text(snapshot_name(s->snap_dir.c_str(), s->snap_fields[k], sl.step, s->snap.z0 + z),
-                                             sl.host + k * per + (size_t)z * s->nx * s->ny, s->nx, s->ny);
-            });
-            for (int v : status)
-                if (v != FDTD_OK)
-                    st = v;
+            if (s->snap.format != FDTD_SNAPSHOT_BINARY) {
+                std::vector<int> status(nf * np, FDTD_OK);
+                parallel_for(nf * np, s->snap.writer_threads, [&](int j) {
+                    const int k = j / np, z = j % np;
+                    status[j] = write_plane_text(
+                        snapshot_name(s->snap_dir.c_str(), s->snap_fields[k], sl.step, s->snap.z0 + z),
+                        sl.host + k * per + (size_t)z * s->nx * s->ny, s->nx, s->ny);
+                });
+                for (int v : status)
+                    if (v != FDTD_OK)
+                        st = v;
+            }
+            if (s->snap.format != FDTD_SNAPSHOT_TEXT)
+                for (int k = 0; k < nf; k++) {
+                    const int v = write_floats(
+                        snapshot_name_f32(s->snap_dir.c_str(), s->snap_fields[k], sl.step, s->snap.z0, np),
+                        sl.host + k * per, per);
+                    if (v != FDTD_OK)
+                        st = v;
+                }
         }
         {
             std::lock_guard<std::mutex> lk(s->mu);
@@ -470,6 +481,8 @@ int fdtd_solver_set_snapshots(fdtd_solver *s, const fdtd_snapshot_spec *spec)
     if (sp.z0 < 0 || sp.nplanes < 0 || sp.z0 + sp.nplanes > s->nz || (sp.field_mask & ((1u << FDTD_FIELD_COUNT) - 1)) == 0)
         return FDTD_ERR_INVALID;
     if (!sp.callback && !sp.output_dir)
+        return FDTD_ERR_INVALID;
+    if (sp.format < FDTD_SNAPSHOT_TEXT || sp.format > FDTD_SNAPSHOT_TEXT_AND_BINARY)
         return FDTD_ERR_INVALID;
     if (s->kernel == FDTD_KERNEL_COMPACT && (sp.field_mask & (7u << FDTD_FIELD_DX)))
         return FDTD_ERR_INVALID;  // D is not stored

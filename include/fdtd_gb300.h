@@ -328,14 +328,24 @@ fdtd_stream_t fdtd_solver_stream(const fdtd_solver *s);
  * host memory that stay valid until the callback returns. */
 typedef void (*fdtd_snapshot_fn)(void *user, int step, int field, const float *data, int z0, int nplanes);
 
+/* Files written when no callback is given.  Text: the reference layout, one
+ * "{H,D,E}_field_{x,y,z}_%05d_z%05d.out" file per field and plane
+ * (writeResults3d, fdtd.cu:1288-1494).  Binary: one
+ * "{H,D,E}_field_{x,y,z}_%05d_z%05d_n%05d.f32" file per field holding the
+ * nplanes x ny x nx floats from plane z0 as they are in memory (little-endian
+ * float32, x fastest): the exact values, for parity checks and fast reading
+ * (no counterpart in the reference). */
+enum { FDTD_SNAPSHOT_TEXT = 0, FDTD_SNAPSHOT_BINARY = 1, FDTD_SNAPSHOT_TEXT_AND_BINARY = 2 };
+
 typedef struct fdtd_snapshot_spec {
     int every;                  /* 0 disables; else every `every` steps */
     uint32_t field_mask;        /* bits 1 << FDTD_FIELD_* */
     int z0, nplanes;            /* z range copied; nplanes 0 = whole volume */
-    fdtd_snapshot_fn callback;  /* NULL: write the reference text layout */
+    fdtd_snapshot_fn callback;  /* NULL: write files under output_dir */
     void *user;
     const char *output_dir;     /* used when callback is NULL */
     int writer_threads;         /* text formatting threads (0 = all cores) */
+    int format;                 /* FDTD_SNAPSHOT_*, used when callback is NULL */
 } fdtd_snapshot_spec;
 
 /* Installs (or with every == 0 removes) the snapshot schedule.  Device-to-host

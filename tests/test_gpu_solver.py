@@ -140,3 +140,24 @@ def test_drop_in_executable_writes_reference_layout(cuda, tmp_path):
         text = (out / f"E_field_z_00002_z{z:05d}.out").read_text()
         want = "".join("".join(" % 9.3E" % float(v) for v in row) + "\n" for row in ez[z])
         assert text == want
+
+
+def test_binary_snapshots_hold_the_exact_fields(cuda, tmp_path):
+    """Text and binary side by side: each .f32 file holds the planes' floats
+    bit for bit, and the text files of the same step format those values."""
+    p, codes, specs, s = solver_from_files(tmp_path, 20, 9, fg.KERNEL_SINGLE_PASS)
+    out = tmp_path / "snap"
+    out.mkdir()
+    s.set_snapshots(every=3, fields=("ez", "hx", "dy"), z0=5, nplanes=4, output_dir=out,
+                    format=fg.SNAPSHOT_TEXT_AND_BINARY)
+    s.run(7)  # snapshots after steps 0, 3, 6
+    s.flush_snapshots()
+    want = s.fields()
+    s.close()
+    for name, tag in (("ez", "E_field_z"), ("hx", "H_field_x"), ("dy", "D_field_y")):
+        raw = np.fromfile(out / f"{tag}_00006_z00005_n00004.f32", dtype="<f4").reshape(4, 20, 20)
+        assert np.array_equal(raw.view(np.uint32), want[name][5:9].view(np.uint32)), name
+        text = (out / f"{tag}_00006_z00007.out").read_text()
+        assert text == "".join("".join(" % 9.3E" % float(v) for v in row) + "\n" for row in raw[2])
+    assert len(list(out.glob("*.f32"))) == 3 * 3
+    assert len(list(out.glob("*.out"))) == 3 * 3 * 4
