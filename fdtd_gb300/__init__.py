@@ -124,6 +124,8 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_setup_mur_uniform", _I, PP, C.c_float, C.c_float, C.c_float, C.c_float, *([_P] * 6))
         _sig(L, "fdtd_read_specs", _I, C.c_char_p, _P)
         _sig(L, "fdtd_load_material_codes", _I, PP, C.c_char_p, C.POINTER(C.c_uint8), _I)
+        _sig(L, "fdtd_load_material_codes_cached", _I, PP, C.c_char_p, C.c_char_p, C.POINTER(C.c_uint8), _I,
+             C.POINTER(_I))
         _sig(L, "fdtd_load_materials", _I, PP, C.c_char_p, C.c_char_p, *([_P] * 4))
         _sig(L, "fdtd_write_results3d", _I, PP, *([_P] * 9), _I, _I)
         _sig(L, "fdtd_copy_symbols", _I, PP)
@@ -265,12 +267,26 @@ def read_specs(path) -> np.ndarray:
     return specs
 
 
-def load_material_codes(p: Params, pgm_dir, nthreads: int = 0) -> np.ndarray:
+def load_material_codes(p: Params, pgm_dir, nthreads: int = 0, cache=None) -> np.ndarray:
+    """uint8 class volume from the PGM slices; with `cache` (a file path),
+    through the binary cache (see load_material_codes_cached)."""
+    if cache is not None:
+        return load_material_codes_cached(p, pgm_dir, cache, nthreads)[0]
     codes = np.zeros(p.shape, np.uint8)
     check(lib().fdtd_load_material_codes(C.byref(p.raw), str(pgm_dir).encode(),
                                          codes.ctypes.data_as(C.POINTER(C.c_uint8)), nthreads),
           "fdtd_load_material_codes")
     return codes
+
+
+def load_material_codes_cached(p: Params, pgm_dir, cache, nthreads: int = 0) -> tuple[np.ndarray, bool]:
+    """(class volume, whether it came from the cache file)."""
+    codes = np.zeros(p.shape, np.uint8)
+    hit = C.c_int(0)
+    check(lib().fdtd_load_material_codes_cached(C.byref(p.raw), str(pgm_dir).encode(), str(cache).encode(),
+                                                codes.ctypes.data_as(C.POINTER(C.c_uint8)), nthreads,
+                                                C.byref(hit)), "fdtd_load_material_codes_cached")
+    return codes, bool(hit.value)
 
 
 def load_materials(p: Params, specs_path, pgm_dir) -> tuple[np.ndarray, ...]:

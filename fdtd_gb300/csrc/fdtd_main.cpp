@@ -19,6 +19,8 @@
 //   --kernel single|two|compact
 //                        fused single-pass, two-pass, or the single-pass compact
 //                        form (nine stored fields: D is not written)
+//   --voxel-cache PATH   read the class volume from a binary cache made by an
+//                        earlier run, or parse the slices and write it
 //   --device N
 #include <chrono>
 #include <cstdio>
@@ -59,7 +61,7 @@ uint32_t parse_fields(const std::string &list)
 
 int main(int argc, char **argv)
 {
-    std::string params_path = "data/input_params", specs_path = "data/mat_specs_riken";
+    std::string params_path = "data/input_params", specs_path = "data/mat_specs_riken", voxel_cache;
     int scheme = FDTD_SCHEME_REFERENCE, every = 1, device = 0, kernel = FDTD_KERNEL_SINGLE_PASS;
     int format = FDTD_SNAPSHOT_TEXT;
     uint32_t mask = (1u << FDTD_FIELD_COUNT) - 1;
@@ -92,9 +94,10 @@ int main(int argc, char **argv)
                                                       : FDTD_KERNEL_SINGLE_PASS;
         }
         else if (a == "--device") device = std::atoi(next());
+        else if (a == "--voxel-cache") voxel_cache = next();
         else {
             std::fprintf(stderr, "usage: %s [--params P] [--specs P] [--scheme reference|corrected] [--every N] "
-                                 "[--fields hx,...] [--format text|binary|both] [--timeskip X] [--kernel single|two|compact] [--device N]\n", argv[0]);
+                                 "[--fields hx,...] [--format text|binary|both] [--timeskip X] [--kernel single|two|compact] [--voxel-cache P] [--device N]\n", argv[0]);
             return 2;
         }
     }
@@ -117,7 +120,11 @@ int main(int argc, char **argv)
     const size_t n = (size_t)p.nx * p.ny * p.nz;
     std::vector<uint8_t> codes(n);
     auto t0 = std::chrono::steady_clock::now();
-    if ((st = fdtd_load_material_codes(&p, p.inputPath, codes.data(), 0)) != FDTD_OK)
+    int cached = 0;
+    st = voxel_cache.empty() ? fdtd_load_material_codes(&p, p.inputPath, codes.data(), 0)
+                             : fdtd_load_material_codes_cached(&p, p.inputPath, voxel_cache.c_str(), codes.data(), 0,
+                                                               &cached);
+    if (st != FDTD_OK)
         return fail("material slices", st);
     int nclasses = 1;
     for (uint8_t c : codes)
@@ -157,7 +164,8 @@ int main(int argc, char **argv)
     auto t2 = std::chrono::steady_clock::now();
     const double setup = std::chrono::duration<double>(t1 - t0).count();
     const double run = std::chrono::duration<double>(t2 - t1).count();
-    std::printf("set-up %.3f s, %d steps %.3f s (%.3e cell-updates/s including output)\n", setup,
+    std::printf("set-up %.3f s%s, %d steps %.3f s (%.3e cell-updates/s including output)\n", setup,
+                voxel_cache.empty() ? "" : cached ? " (voxels from cache)" : " (voxel cache written)",
                 p.iterationsCount, run, (double)n * p.iterationsCount / run);
     fdtd_solver_destroy(s);
     fdtd_params_free(&p);

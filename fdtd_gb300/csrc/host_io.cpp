@@ -14,6 +14,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+
+#include <sys/stat.h>
 #include <thread>
 #include <vector>
 
@@ -414,6 +416,73 @@ int fdtd_load_material_codes(const FdtdParams *p, const char *materialsPath, uin
     for (int st : status)
         if (st != FDTD_OK)
             return st;
+    return FDTD_OK;
+}
+
+int fdtd_load_material_codes_cached(const FdtdParams *p, const char *materialsPath, const char *cachePath,
+                                    uint8_t *codes, int nthreads, int *fromCache)
+{
+    if (fromCache)
+        *fromCache = 0;
+    if (!p || !materialsPath || !cachePath || !codes || p->nx <= 0 || p->ny <= 0 || p->nz <= 0)
+        return FDTD_ERR_INVALID;
+    // fingerprint of the slice files: FNV-1a over the dimensions and each
+    // slice's size and modification time (a missing slice makes the parse fail)
+    unsigned long long fp = 1469598103934665603ULL;
+    auto mix = [&](unsigned long long v) {
+        for (int b = 0; b < 8; b++)
+            fp = (fp ^ ((v >> (8 * b)) & 0xffu)) * 1099511628211ULL;
+    };
+    mix((unsigned long long)p->nx);
+    mix((unsigned long long)p->ny);
+    mix((unsigned long long)p->nz);
+    for (int z = 0; z < p->nz; z++) {
+        char name[64];
+        std::snprintf(name, sizeof name, "/v1_%05d.pgm", z + 1);
+        struct stat sb;
+        if (stat((std::string(materialsPath) + name).c_str(), &sb) != 0)
+            return FDTD_ERR_IO;
+        mix((unsigned long long)sb.st_size);
+        mix((unsigned long long)sb.st_mtim.tv_sec);
+        mix((unsigned long long)sb.st_mtim.tv_nsec);
+    }
+    static const char MAGIC[8] = {'F', 'D', 'T', 'D', 'U', '8', 'V', '1'};
+    struct Header {
+        char magic[8];
+        int32_t nx, ny, nz, pad;
+        uint64_t fingerprint;
+    };
+    const size_t n = (size_t)p->nx * p->ny * p->nz;
+    if (FILE *f = std::fopen(cachePath, "rb")) {
+        Header h{};
+        const bool hit = std::fread(&h, sizeof h, 1, f) == 1 && std::memcmp(h.magic, MAGIC, 8) == 0 &&
+                         h.nx == p->nx && h.ny == p->ny && h.nz == p->nz && h.fingerprint == fp &&
+                         std::fread(codes, 1, n, f) == n;
+        std::fclose(f);
+        if (hit) {
+            if (fromCache)
+                *fromCache = 1;
+            return FDTD_OK;
+        }
+    }
+    const int st = fdtd_load_material_codes(p, materialsPath, codes, nthreads);
+    if (st != FDTD_OK)
+        return st;
+    // write beside the target and rename, so a reader never sees half a cache
+    const std::string tmp = std::string(cachePath) + ".tmp";
+    if (FILE *f = std::fopen(tmp.c_str(), "wb")) {
+        Header h{};
+        std::memcpy(h.magic, MAGIC, 8);
+        h.nx = p->nx;
+        h.ny = p->ny;
+        h.nz = p->nz;
+        h.fingerprint = fp;
+        const bool ok = std::fwrite(&h, sizeof h, 1, f) == 1 && std::fwrite(codes, 1, n, f) == n;
+        if (std::fclose(f) == 0 && ok)
+            std::rename(tmp.c_str(), cachePath);
+        else
+            std::remove(tmp.c_str());
+    }
     return FDTD_OK;
 }
 

@@ -131,6 +131,16 @@ int fdtd_read_specs(const char *specsPath, float *specs);
 int fdtd_load_material_codes(const FdtdParams *p, const char *materialsPath, uint8_t *codes,
                              int nthreads);
 
+/* fdtd_load_material_codes through a binary cache of the class volume (no
+ * counterpart in the reference, which parses its nz text slices on every
+ * run).  When cachePath holds a volume of these dimensions made from slice
+ * files of the same sizes and modification times, the volume is read from
+ * it; otherwise the slices are parsed and the cache is (re)written, on a
+ * best-effort basis (a cache that cannot be written is not an error).
+ * *fromCache (optional) receives 1 when the cache was used, else 0. */
+int fdtd_load_material_codes_cached(const FdtdParams *p, const char *materialsPath, const char *cachePath,
+                                    uint8_t *codes, int nthreads, int *fromCache);
+
 /* Replaces loadMaterials (fdtd.cu:875-939) in the reference's form: four
  * per-cell float arrays looked up from the specs table. */
 int fdtd_load_materials(const FdtdParams *p, const char *specsPath, const char *materialsPath,

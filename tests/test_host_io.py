@@ -172,3 +172,42 @@ def test_phantom_writer_round_trip(tmp_path):
     assert np.array_equal(codes, ph.sphere_phantom(16, 4.0))
     specs = fg.read_specs(tmp_path / "mat_specs")
     np.testing.assert_array_equal(specs[1], np.float32([0.5, 50.0, 4.0, 8e-12]))
+
+
+def test_voxel_cache_hit_miss_and_invalidation(golden, tmp_path):
+    """The first load parses the slices and writes the cache; the second reads
+    the cache; touching a slice (new size or time) or asking for other
+    dimensions makes it parse again.  Every load equals the parsed volume."""
+    import os
+
+    z, p, pgm = _write_golden_phantom(golden, tmp_path)
+    cache = tmp_path / "codes.u8v"
+    codes, hit = fg.load_material_codes_cached(p, pgm, cache)
+    assert not hit and cache.exists()
+    assert np.array_equal(codes, z["codes"])
+    assert cache.stat().st_size == 32 + codes.size
+    codes, hit = fg.load_material_codes_cached(p, pgm, cache, nthreads=2)
+    assert hit and np.array_equal(codes, z["codes"])
+    assert np.array_equal(fg.load_material_codes(p, pgm, cache=cache), z["codes"])
+    # a slice rewritten with another class: its time changes, so the cache is stale
+    first = sorted(pgm.iterdir())[0]
+    text = first.read_text()
+    lines = text.split("\n")
+    body = " ".join(lines[4:]).split()
+    body[0] = "0" if body[0] != "0" else "1"
+    first.write_text("\n".join(lines[:4]) + "\n" + " ".join(body) + "\n")
+    st = first.stat()
+    os.utime(first, ns=(st.st_atime_ns, st.st_mtime_ns + 1_000_000_000))
+    codes, hit = fg.load_material_codes_cached(p, pgm, cache)
+    assert not hit
+    assert np.array_equal(codes, fg.load_material_codes(p, pgm))
+    assert not np.array_equal(codes, z["codes"])
+    # a truncated cache is a miss, never an error
+    cache.write_bytes(cache.read_bytes()[:40])
+    codes2, hit = fg.load_material_codes_cached(p, pgm, cache)
+    assert not hit and np.array_equal(codes2, codes)
+    _, hit = fg.load_material_codes_cached(p, pgm, cache)
+    assert hit
+    # an unwritable cache path still loads
+    codes3, hit = fg.load_material_codes_cached(p, pgm, tmp_path / "no_dir" / "c.u8v")
+    assert not hit and np.array_equal(codes3, codes)
