@@ -126,7 +126,7 @@ int rebuild(fdtd_batch *b)
             if (!encode_step_maps(d.c[par], b->compact, &d.maps[par]))
                 return FDTD_ERR_INVALID;
         }
-        d.zchunk = fused_zchunk(v->nz);
+        d.zchunk = b->compact ? compact_zchunk(v->nz) : fused_zchunk(v->nz);
         d.tiles_x = (v->nx + 31) / 32;
         d.tiles_y = (v->ny + ty - 1) / ty;
         d.chunks = (v->nz + d.zchunk - 1) / d.zchunk;

@@ -339,11 +339,13 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     g0 = tcy * (hzn - hnr(2, ty, tx + 1)) - tcz * (hyn - hym);
                 if (dy_on)
                     g1 = tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
-                // the per-cell test over the source list measured faster than the
-                // column mask in this form (5 % on the 512x512x400 phantom)
+                // the per-cell test over the source list, in units that hold a
+                // source only, measured faster than the column mask in this form
+                // (which needs three more registers of the 48)
                 bool src = false;
-                for (int s = 0; s < c.nsources; s++)
-                    src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
+                if (unit_src)
+                    for (int s = 0; s < c.nsources; s++)
+                        src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
                 if (dz_on || src) {
                     g2 = tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
                     if (src)
@@ -655,6 +657,13 @@ __global__ void batch_advance_kernel(const BatchDesc *__restrict__ descs, int ns
 #ifndef FDTD_RING_STAGES
 #define FDTD_RING_STAGES 3
 #endif
+// Largest z chunk of the compact form.  Its CTAs run at about 1.3x the D
+// form's cell rate; with chunks of 24 planes or more its DRAM throughput fell
+// on grids above 100 M cells (0.86 of the copy bandwidth at 24 planes, 0.80
+// at 64) while 16-20 planes held 0.96-0.99 from 105 M to 537 M cells.
+#ifndef FDTD_COMPACT_ZCHUNK
+#define FDTD_COMPACT_ZCHUNK 16
+#endif
 constexpr int TY_SEL = FDTD_TILE_ROWS;
 constexpr int S_SEL = FDTD_RING_STAGES;
 
@@ -688,14 +697,27 @@ int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 
 }  // namespace
 
+// nz split into equal chunks of at most max_planes planes
+static int zchunk_of(int nz, int max_planes)
+{
+    const int chunks = (nz + max_planes - 1) / max_planes;
+    return (nz + chunks - 1) / chunks;
+}
+
+#ifndef FDTD_ZCHUNK
+#define FDTD_ZCHUNK 64
+#endif
+static_assert(FDTD_ZCHUNK >= 4 && FDTD_ZCHUNK <= 64, "a unit's per-thread source mask covers 66 planes");
+
 int fused_zchunk(int nz)
 {
     // about 64 planes per CTA: enough CTAs per wave on 152 SMs, little
     // prologue/epilogue traffic at chunk borders.  At most 64: a unit's
     // per-thread source mask covers 66 planes.
-    const int chunks = (nz + 63) / 64;
-    return (nz + chunks - 1) / chunks;
+    return zchunk_of(nz, FDTD_ZCHUNK);
 }
+
+int compact_zchunk(int nz) { return zchunk_of(nz, FDTD_COMPACT_ZCHUNK); }
 
 bool fused_uses_tma(const NativeConsts &c)
 {
@@ -798,9 +820,10 @@ int launch_h_e_compact(const NativeConsts &c, cudaStream_t s)
 {
     if (c.d_cur[0] != c.d_prev[0] || c.d_cur[1] != c.d_prev[1] || c.d_cur[2] != c.d_prev[2])
         return FDTD_ERR_INVALID;  // R is updated in place
+    static_assert(FDTD_COMPACT_ZCHUNK >= 4, "z chunks hold at least four planes");
     FusedArgs a;
     a.c = c;
-    a.zchunk = fused_zchunk(c.nz);
+    a.zchunk = compact_zchunk(c.nz);  // the compact form reads no source-plane mask
     FusedMaps maps;
     if (encode_step_maps(c, true, &maps))
         return launch_fused_impl<true, true>(a, maps, s);

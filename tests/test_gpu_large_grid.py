@@ -3,8 +3,7 @@ the compact form, 160 GB in the D form): all 64-bit index paths.  A source
 and a small Debye block sit near the far corner, so the cells around them have
 indices beyond 2^31.  For 12 steps the fields there depend only on cells
 within reach of the wave, so they must equal those of a 64^3 grid holding
-the same local problem at the same position relative to the 32x8 tiles and
-the z chunks."""
+the same local problem at the same position relative to the 32x8 tiles."""
 from __future__ import annotations
 
 import numpy as np
@@ -17,8 +16,11 @@ from .gpu_util import Params, make_params
 pytestmark = pytest.mark.gpu
 
 BIG, SMALL = (1300, 1300, 1300), (64, 64, 64)
-# source positions: same lane, same row within the tile, same offset within the z chunk
-# (1300 planes make chunks of 62 from 1240; 64 planes make one chunk)
+# source positions: same lane, same row within the tile and, for the D form,
+# the same offset within the z chunk (1300 planes make chunks of 62 from 1240;
+# 64 planes make one chunk).  The compact form's 16-plane chunks put the
+# source at offset 0 (big) and 8 (small); the update of a cell does not depend
+# on where the chunk borders lie.
 SRC_BIG, SRC_SMALL = (1280, 1280, 1280), (32, 32, 40)
 STEPS = 12
 

@@ -18,7 +18,7 @@ from .helpers import assert_fields_close, class_media, random_case
 
 pytestmark = pytest.mark.gpu
 
-DIMS = (160, 48, 140)  # 5 x 6 tiles, 3 z chunks: inner CTAs exist
+DIMS = (160, 48, 140)  # 5 x 6 tiles; 3 z chunks (D form) or 9 (compact form): inner CTAs exist
 
 
 @pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT])
@@ -55,10 +55,13 @@ def test_sources_on_z_chunk_borders(cuda, kernel):
     (which the next chunk also stages, to recompute H below its first plane),
     the first plane of the next chunk, and a pair on the planes either side of
     a border; against the FP64 oracle."""
-    dims = (70, 26, 150)          # z chunks of 50 planes: [0, 50), [50, 100), [100, 150)
+    dims = (70, 26, 150)
+    # nz is split into equal chunks of at most 64 planes (D form: 3 of 50) or
+    # at most 16 (compact form: 10 of 15)
+    zc = 50 if kernel == fg.KERNEL_SINGLE_PASS else 15
     steps = 60
     codes, specs, rp, _, consts, jz = random_case(*dims, seed=5, ncls=3, nsrc=0)
-    sources = [(35, 13, 49), (20, 7, 50), (50, 20, 99), (40, 10, 100), (41, 11, 101)]
+    sources = [(35, 13, zc - 1), (20, 7, zc), (50, 20, 2 * zc - 1), (40, 10, 2 * zc), (41, 11, 2 * zc + 1)]
     raw = make_params(dims, consts, sources, jz)
     with fg.Solver(Params(raw), codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel) as s:
         s.run(steps)
