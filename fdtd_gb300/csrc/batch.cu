@@ -137,7 +137,7 @@ int rebuild(fdtd_batch *b)
         for (int f = 0; f < 12; f++) {
             const MurFace m = mur_face(f, v->nx, v->ny, v->nz);
             const long long cells = (long long)m.len_u * m.len_v;
-            for (long long first = 0; first < cells; first += 256)
+            for (long long first = 0; first < cells; first += BATCH_MUR_CELLS)
                 mur.push_back(BatchMurBlock{(int)i, f, (int)first, 0});
         }
     }

@@ -145,6 +145,58 @@ __device__ __forceinline__ void mur_apply(int f, int iu, int iv, int nx, int ny,
     T[i] = mur_value(dt, h, me, rs, rn, t_nbr, S[j], S[i]);
 }
 
+// Indices of one face cell at face coordinates (u, v): the cell, its inward
+// neighbour and its two Mur slab entries (self, neighbour).
+struct MurCellIdx {
+    size_t face, nbr, rs, rn;
+};
+
+__device__ __forceinline__ MurCellIdx mur_cell_idx(const MurFace &m, int u, int v, int nx, int ny, int nz, int pitch)
+{
+    const int ks = m.far ? 1 : 0, kn = m.far ? 0 : 1;
+    int x, y, z, dxn = 0, dyn = 0, dzn = 0;
+    MurCellIdx c;
+    if (m.axis == 0) {
+        x = m.far ? nx - 1 : 0; y = u; z = v; dxn = m.far ? -1 : 1;
+        c.rs = ((size_t)z * ny + y) * 2 + ks;
+        c.rn = ((size_t)z * ny + y) * 2 + kn;
+    } else if (m.axis == 1) {
+        x = u; y = m.far ? ny - 1 : 0; z = v; dyn = m.far ? -1 : 1;
+        c.rs = ((size_t)z * 2 + ks) * nx + x;
+        c.rn = ((size_t)z * 2 + kn) * nx + x;
+    } else {
+        x = u; y = v; z = m.far ? nz - 1 : 0; dzn = m.far ? -1 : 1;
+        c.rs = ((size_t)ks * ny + y) * nx + x;
+        c.rn = ((size_t)kn * ny + y) * nx + x;
+    }
+    c.face = cell_index(x, y, z, pitch, ny);
+    c.nbr = cell_index(x + dxn, y + dyn, z + dzn, pitch, ny);
+    return c;
+}
+
+// Operands of one face set: target / source arrays of its component, the
+// array its neighbour term reads, its cell size and its slab.
+struct MurSet {
+    const MurFace m;
+    float *T;
+    const float *S, *TN, *slab;
+    float h;
+    __device__ __forceinline__ MurSet(int f, int nx, int ny, int nz, float hx, float hy, float hz, const MurSlabs &rp,
+                                      float *t0, float *t1, float *t2, const float *s0, const float *s1,
+                                      const float *s2, bool fix_ey)
+        : m(mur_face(f, nx, ny, nz))
+    {
+        S = m.comp == 0 ? s0 : (m.comp == 1 ? s1 : s2);
+        T = m.comp == 0 ? t0 : (m.comp == 1 ? t1 : t2);
+        const bool quirk = m.comp == 1 && m.axis == 0 && m.far && !fix_ey;  // fdtd_calculations.cu:323
+        TN = quirk ? S : T;
+        h = m.axis == 0 ? hx : (m.axis == 1 ? hy : hz);
+        slab = m.axis == 0 ? (m.far ? rp.rpx_end : rp.rpx0)
+               : m.axis == 1 ? (m.far ? rp.rpy_end : rp.rpy0)
+                             : (m.far ? rp.rpz_end : rp.rpz0);
+    }
+};
+
 // mur_apply for K cells of one face set at in-face rows iv0, iv0 + vstride,
 // ... below v_end: all loads are issued before any store, so K independent loads per
 // array are in flight per thread (face cells are written, their neighbours
@@ -156,19 +208,11 @@ __device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride,
                                             float *t0, float *t1, float *t2, const float *s0, const float *s1,
                                             const float *s2, bool fix_ey)
 {
-    const MurFace m = mur_face(f, nx, ny, nz);
+    const MurSet ms(f, nx, ny, nz, hx, hy, hz, rp, t0, t1, t2, s0, s1, s2, fix_ey);
+    const MurFace &m = ms.m;
     if (iu >= m.len_u)
         return;
     const int u = m.u0 + iu;
-    const float *S = m.comp == 0 ? s0 : (m.comp == 1 ? s1 : s2);
-    float *T = m.comp == 0 ? t0 : (m.comp == 1 ? t1 : t2);
-    const bool quirk = m.comp == 1 && m.axis == 0 && m.far && !fix_ey;  // fdtd_calculations.cu:323
-    const float *TN = quirk ? S : T;
-    const float h = m.axis == 0 ? hx : (m.axis == 1 ? hy : hz);
-    const float *slab = m.axis == 0 ? (m.far ? rp.rpx_end : rp.rpx0)
-                        : m.axis == 1 ? (m.far ? rp.rpy_end : rp.rpy0)
-                                      : (m.far ? rp.rpz_end : rp.rpz0);
-    const int ks = m.far ? 1 : 0, kn = m.far ? 0 : 1;
     float rs[K], rn[K], tn[K], sn[K], sf[K];
     size_t face[K];
     bool on[K];
@@ -176,36 +220,58 @@ __device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride,
     for (int k = 0; k < K; k++) {
         const int iv = iv0 + k * vstride;
         on[k] = iv < m.len_v && iv < v_end;
-        const int v = m.v0 + (on[k] ? iv : 0);
-        int x, y, z, dxn = 0, dyn = 0, dzn = 0;
-        size_t rs_i, rn_i;
-        if (m.axis == 0) {
-            x = m.far ? nx - 1 : 0; y = u; z = v; dxn = m.far ? -1 : 1;
-            rs_i = ((size_t)z * ny + y) * 2 + ks;
-            rn_i = ((size_t)z * ny + y) * 2 + kn;
-        } else if (m.axis == 1) {
-            x = u; y = m.far ? ny - 1 : 0; z = v; dyn = m.far ? -1 : 1;
-            rs_i = ((size_t)z * 2 + ks) * nx + x;
-            rn_i = ((size_t)z * 2 + kn) * nx + x;
-        } else {
-            x = u; y = v; z = m.far ? nz - 1 : 0; dzn = m.far ? -1 : 1;
-            rs_i = ((size_t)ks * ny + y) * nx + x;
-            rn_i = ((size_t)kn * ny + y) * nx + x;
-        }
-        face[k] = cell_index(x, y, z, pitch, ny);
-        const size_t j = cell_index(x + dxn, y + dyn, z + dzn, pitch, ny);
+        const MurCellIdx c = mur_cell_idx(m, u, m.v0 + (on[k] ? iv : 0), nx, ny, nz, pitch);
+        face[k] = c.face;
         if (on[k]) {
-            rs[k] = slab[rs_i];
-            rn[k] = slab[rn_i];
-            tn[k] = TN[j];
-            sn[k] = S[j];
-            sf[k] = S[face[k]];
+            rs[k] = ms.slab[c.rs];
+            rn[k] = ms.slab[c.rn];
+            tn[k] = ms.TN[c.nbr];
+            sn[k] = ms.S[c.nbr];
+            sf[k] = ms.S[c.face];
         }
     }
 #pragma unroll
     for (int k = 0; k < K; k++)
         if (on[k])
-            T[face[k]] = mur_value(dt, h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
+            ms.T[face[k]] = mur_value(dt, ms.h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
+}
+
+// mur_apply for K cells of one face set at flat in-face indices idx0,
+// idx0 + stride, ... (row-major over (v, u), below len_u * len_v < 2^31);
+// loads before stores as in mur_apply_k.
+template <int K>
+__device__ __forceinline__ void mur_apply_flat_k(int f, unsigned idx0, unsigned stride, int nx, int ny, int nz,
+                                                 int pitch, float dt, float hx, float hy, float hz, float me,
+                                                 const MurSlabs &rp, float *t0, float *t1, float *t2,
+                                                 const float *s0, const float *s1, const float *s2, bool fix_ey)
+{
+    const MurSet ms(f, nx, ny, nz, hx, hy, hz, rp, t0, t1, t2, s0, s1, s2, fix_ey);
+    const MurFace &m = ms.m;
+    if (m.len_u <= 0 || m.len_v <= 0)
+        return;
+    const unsigned lu = (unsigned)m.len_u, total = lu * (unsigned)m.len_v;
+    float rs[K], rn[K], tn[K], sn[K], sf[K];
+    size_t face[K];
+    bool on[K];
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+        const unsigned idx = idx0 + (unsigned)k * stride;
+        on[k] = idx < total;
+        const unsigned i = on[k] ? idx : 0u;
+        const MurCellIdx c = mur_cell_idx(m, m.u0 + (int)(i % lu), m.v0 + (int)(i / lu), nx, ny, nz, pitch);
+        face[k] = c.face;
+        if (on[k]) {
+            rs[k] = ms.slab[c.rs];
+            rn[k] = ms.slab[c.rn];
+            tn[k] = ms.TN[c.nbr];
+            sn[k] = ms.S[c.nbr];
+            sf[k] = ms.S[c.face];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < K; k++)
+        if (on[k])
+            ms.T[face[k]] = mur_value(dt, ms.h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
 }
 
 }  // namespace fdtd

@@ -117,7 +117,10 @@ struct alignas(64) BatchDesc {
     int pad;
 };
 
-// One face block of the batched Mur launch: solve, face set, first cell.
+// One face block of the batched Mur launch: solve, face set, first cell;
+// a block of 256 threads updates BATCH_MUR_CELLS consecutive cells of the set.
+constexpr int BATCH_MUR_CELLS = 1024;
+static_assert(BATCH_MUR_CELLS % 256 == 0, "whole cells per thread");
 struct BatchMurBlock {
     int solve, face, first, pad;
 };

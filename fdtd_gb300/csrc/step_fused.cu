@@ -626,14 +626,12 @@ __global__ void __launch_bounds__(256) batch_mur_kernel(const BatchDesc *__restr
     if (n >= d.steps_target)
         return;
     const NativeConsts &c = d.c[n & 1];
-    const MurFace m = mur_face(b.face, c.nx, c.ny, c.nz);
-    const unsigned idx = (unsigned)b.first + threadIdx.x;  // faces of batched solves hold < 2^31 cells
-    if ((long long)idx >= (long long)m.len_u * m.len_v)
-        return;
-    const unsigned lu = (unsigned)m.len_u;
-    mur_apply(b.face, (int)(idx % lu), (int)(idx / lu), c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz,
-              c.me, c.rp, c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
-              c.scheme == FDTD_SCHEME_CORRECTED);
+    // BATCH_MUR_CELLS cells from b.first: thread t takes first + t + k * 256
+    // (faces of batched solves hold < 2^31 cells)
+    mur_apply_flat_k<BATCH_MUR_CELLS / 256>(b.face, (unsigned)b.first + threadIdx.x, 256u, c.nx, c.ny, c.nz, c.pitch,
+                                            c.dt, c.hx, c.hy, c.hz, c.me, c.rp, c.e_prev[0], c.e_prev[1],
+                                            c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
+                                            c.scheme == FDTD_SCHEME_CORRECTED);
 }
 
 __global__ void batch_advance_kernel(const BatchDesc *__restrict__ descs, int nsolves, int *work_counter)
