@@ -214,28 +214,30 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
     if (!TMA && in_dom && zc0 < nz)
         mat_next = c.mat[(size_t)zc0 * plane + col];
 
+    // a bounded wait gave up: raise the error flag, let the copies in flight
+    // land (bounded) and leave; called by every thread after one CTA-wide
+    // decision, so no thread is left at a barrier
+    auto give_up = [&](int k) {
+        if (tid == 0) {
+            atomicExch(c.err, 1);
+            for (int j = k; j < nplanes && j < k + S; j++)
+                mbar_wait(bar(j), parity(j));
+        }
+        __syncthreads();
+    };
     for (int k = 0; k < nplanes; k++) {
         const int z = p0 + k;
         if (z >= zc1)
             break;
         // planes k and k+1 resident
+        bool ok = true;
         if (TMA) {
-            bool ok = true;
             if (k == 0)
                 ok = mbar_wait(bar(0), parity(0));
             if (ok && k + 1 < nplanes)
                 ok = mbar_wait(bar(k + 1), parity(k + 1));
-            // one decision for the whole CTA, so no thread is left at a barrier
-            if (__syncthreads_or(!ok)) {
-                if (tid == 0) {
-                    atomicExch(c.err, 1);
-                    // let the copies in flight land before the CTA exits (bounded)
-                    for (int j = k; j < nplanes && j < k + S; j++)
-                        mbar_wait(bar(j), parity(j));
-                }
-                __syncthreads();
-                return false;
-            }
+            // the CTA decides at its next barrier (below): until then it only
+            // reads shared memory
         } else {
             cp_async_wait<S - 2>();
             __syncthreads();
@@ -292,7 +294,8 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     hnr(2, row + 1, 0) = v;
                 }
             }
-            // low-y halo row: hx, hz at y - 1
+            // low-y halo row: hx, hz at y - 1 (decision point below: nothing
+            // is written to global memory before it)
             if (ty == 0 && y >= 1 && x < nx) {
                 const int r = 0, cc = tx + 4;  // y - 1
                 const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
@@ -305,7 +308,14 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
                 hnr(2, 0, tx + 1) = v;
             }
-            __syncthreads();
+            if (TMA) {
+                if (__syncthreads_or(!ok)) {
+                    give_up(k);
+                    return false;
+                }
+            } else {
+                __syncthreads();
+            }
 
             float ey_new = 0.0f, ez_new = 0.0f;  // this lane's E^{n+1} y, z (for the x-face lanes)
             if constexpr (COMPACT) {
@@ -463,7 +473,14 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             hxm = hxn;
             hym = hyn;
         }
-        __syncthreads();  // stage k and hn fully consumed
+        if (TMA && z < zc0) {  // the chunk prologue plane has no other decision point
+            if (__syncthreads_or(!ok)) {
+                give_up(k);
+                return false;
+            }
+        } else {
+            __syncthreads();  // stage k and hn fully consumed
+        }
         // refill the stage of plane k with plane k + S
         const int kn = k + S;
         if (TMA) {
