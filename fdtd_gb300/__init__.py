@@ -145,6 +145,7 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_solver_destroy", _I, _V)
         _sig(L, "fdtd_solver_run", _I, _V, _I)
         _sig(L, "fdtd_solver_synchronize", _I, _V)
+        _sig(L, "fdtd_solver_test_stall", _I, _V)
         _sig(L, "fdtd_solver_steps", _I, _V)
         _sig(L, "fdtd_solver_get_field", _I, _V, _I, _P)
         _sig(L, "fdtd_solver_stream", _V, _V)
@@ -333,6 +334,11 @@ class Solver:
 
     def synchronize(self) -> None:
         check(lib().fdtd_solver_synchronize(self.handle), "fdtd_solver_synchronize")
+
+    def test_stall(self) -> None:
+        """Failure-path test hook: the next single-pass step's first CTA lets one
+        bounded wait run out; synchronize() then raises FDTD_ERR_DEVICE_TIMEOUT."""
+        check(lib().fdtd_solver_test_stall(self.handle), "fdtd_solver_test_stall")
 
     @property
     def steps(self) -> int:

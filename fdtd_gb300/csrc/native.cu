@@ -99,6 +99,7 @@ NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)
     c.step = n;
     c.step_counter = nullptr;
     c.err = p->d_err;
+    c.stall_once = p->d_stall;
     if (f) {
         for (int k = 0; k < 3; k++) {
             c.h_in[k] = (&f->hx)[k];
@@ -418,6 +419,7 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
         rpd[k] = reinterpret_cast<float *>(base + offs[2 + k]);
     plan->rp = MurSlabs{rpd[0], rpd[1], rpd[2], rpd[3], rpd[4], rpd[5]};
     plan->d_err = reinterpret_cast<int *>(base + err_off);
+    plan->d_stall = plan->d_err + 1;
     plan->d_mur_x = reinterpret_cast<float4 *>(base + murx_off);
     {
         // The x-face Mur factors of mur_value, rounded one operation at a time
@@ -444,7 +446,7 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
         e = cudaMemcpy(plan->d_mur_x, murx.data(), sizeof(float4) * nmurx, cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess)
-        e = cudaMemset(plan->d_err, 0, sizeof(int));
+        e = cudaMemset(plan->d_err, 0, 2 * sizeof(int));  // error flag, test hook word
     if (e == cudaSuccess)
         e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)

@@ -23,6 +23,7 @@ struct fdtd_plan {
     fdtd::MurSlabs rp{};                  // six Mur slabs
     float4 *d_mur_x = nullptr;            // x-face Mur coefficients, [face][z][y] (see mur_x_coef)
     int *d_err = nullptr;                 // device error flag
+    int *d_stall = nullptr;               // test hook word (NativeConsts::stall_once)
 };
 
 namespace fdtd {
@@ -46,6 +47,9 @@ struct NativeConsts {
     int step;              // step index n when step_counter is null
     int *step_counter;     // device step index (graph replay), may be null
     int *err;              // device error flag (a bounded wait gave up)
+    int *stall_once;       // test hook, may be null: when set, the first CTA of the next single-pass
+                           // launch clears it and arms one plane's barrier without issuing its
+                           // copies, so that CTA's bounded wait runs out (raises *err)
     int overlap_prev;      // single-pass launch may start while the previous step's Mur kernel runs
                            // (programmatic dependent launch; only where that kernel precedes it)
     int fuse_mur_x;        // the single-pass kernel applies the x-face Mur updates and the Mur

@@ -446,6 +446,18 @@ int fdtd_solver_synchronize(fdtd_solver *s)
 
 int fdtd_solver_steps(const fdtd_solver *s) { return s ? s->steps : -1; }
 
+int fdtd_solver_test_stall(fdtd_solver *s)
+{
+    if (!s)
+        return FDTD_ERR_INVALID;
+    cudaSetDevice(s->device);
+    static const int one = 1;
+    int st = cu(cudaMemcpyAsync(s->plan->d_stall, &one, sizeof one, cudaMemcpyHostToDevice, s->stream));
+    if (st == FDTD_OK)
+        st = cu(cudaStreamSynchronize(s->stream));  // the source is host memory of this call
+    return st;
+}
+
 fdtd_stream_t fdtd_solver_stream(const fdtd_solver *s) { return s ? s->stream : nullptr; }
 
 int fdtd_solver_get_field(fdtd_solver *s, int field, float *host_out)

@@ -61,13 +61,17 @@ struct FusedArgs {
 };
 
 // TMA: one thread arms the stage's barrier and issues the plane's boxes.
+// With arm_only (the stall test hook) the barrier expects the plane's bytes
+// but no copy is issued.
 template <int TY, int NT = 9>
 __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
-                                int z)
+                                int z, bool arm_only = false)
 {
     using G = Geo<TY, NT>;
     const unsigned bytes = kind == PLANE_FULL ? G::TX_FULL : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI);
     mbar_expect_tx(bar, bytes);
+    if (arm_only)
+        return;
     for (int c = 0; c < 3; c++)
         tma_load_3d(smem_addr(stage + G::OFF_E + c * pad128(G::E_BYTES)), &maps.m[c], x0 - 4, y0 - 1, z, bar);
     if (kind == PLANE_EPI)
@@ -130,11 +134,12 @@ __device__ __forceinline__ bool unit_has_source(const NativeConsts &c, int x0, i
 // One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
 // stage ring and its barriers continue from earlier units of the same CTA:
 // g0 counts the planes this CTA has staged before.  Returns false when a
-// bounded wait gave up (the error flag is set; the CTA must stop).
+// bounded wait gave up (the error flag is set; the CTA must stop).  stall
+// (read by thread 0 only): leave the second plane's copies unissued.
 template <int TY, int S, bool TMA, bool COMPACT = false>
 __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMaps &maps, int zchunk, int bx, int by,
                                            int bz, unsigned char *smem, const DebyeCoef *coef, uint64_t *bars,
-                                           unsigned g0)
+                                           unsigned g0, bool stall = false)
 {
     constexpr int NT = COMPACT ? 3 : 9;
     using G = Geo<TY, NT>;
@@ -157,7 +162,8 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             const int z = p0 + k;
             if (TMA) {
                 if (tid == 0)
-                    issue_plane_tma<TY, NT>(maps, stage(k), bar(k), plane_kind(z, zc0, zc1), x0, y0, z);
+                    issue_plane_tma<TY, NT>(maps, stage(k), bar(k), plane_kind(z, zc0, zc1), x0, y0, z,
+                                            stall && k == 1);
             } else {
                 issue_plane_generic<TY, NT>(c, stage(k), plane_kind(z, zc0, zc1), x0, y0, z, tid);
             }
@@ -565,7 +571,11 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
             asm volatile("griddepcontrol.wait;" ::: "memory");
     }
     __syncthreads();
-    fused_unit<TY, S, TMA, COMPACT>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, smem, coef, bars, 0u);
+    bool stall = false;
+    if (TMA && a.c.stall_once && blockIdx.x == 0 && blockIdx.y == 0 && bz == 0 && threadIdx.x == 0 &&
+        threadIdx.y == 0)
+        stall = atomicExch(a.c.stall_once, 0) != 0;
+    fused_unit<TY, S, TMA, COMPACT>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, smem, coef, bars, 0u, stall);
 }
 
 // Many solves: persistent CTAs take work units from a counter; a unit's solve

@@ -138,6 +138,7 @@ extern "C" int fdtd_step_static(const FdtdParams *p, const float *specs, int ncl
     c.step = 0;
     c.step_counter = nullptr;
     c.err = d_err;
+    c.stall_once = nullptr;
     c.rp = MurSlabs{rp_dev[0], rp_dev[1], rp_dev[2], rp_dev[3], rp_dev[4], rp_dev[5]};
     for (int k = 0; k < 3; k++) {
         c.h_in[k] = (&f->hx)[k];

@@ -14,6 +14,7 @@ namespace tma {
 
 constexpr int FTX = 32;            // tile width in x (one warp)
 constexpr int MBAR_SPIN_LIMIT = 1 << 22;
+constexpr unsigned long long MBAR_WAIT_NS = 200000000ull;  // a wait gives up after 0.2 s
 
 __host__ __device__ constexpr int pad128(int bytes) { return (bytes + 127) & ~127; }
 
@@ -45,12 +46,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: false after MBAR_SPIN_LIMIT polls.
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait: false after MBAR_WAIT_NS of the global timer (read every
+// 256 polls once the first poll failed) or MBAR_SPIN_LIMIT polls.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 {
-    for (int i = 0; i < MBAR_SPIN_LIMIT; i++)
+    if (mbar_try_wait(bar, parity))
+        return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (int i = 1; i < MBAR_SPIN_LIMIT; i++) {
         if (mbar_try_wait(bar, parity))
             return true;
+        if ((i & 255) == 0 && globaltimer_ns() - t0 > MBAR_WAIT_NS)
+            return false;
+    }
     return false;
 }
 

@@ -326,6 +326,14 @@ int fdtd_solver_synchronize(fdtd_solver *s);
 /* Number of completed-or-enqueued steps. */
 int fdtd_solver_steps(const fdtd_solver *s);
 
+/* Test hook of the failure path (no counterpart in the reference): the next
+ * single-pass step launched with TMA staging has its first CTA arm one plane's
+ * barrier without issuing the copies, so that CTA's bounded wait (0.2 s) runs
+ * out; the CTA raises the solver's error flag and exits, the launch completes,
+ * and fdtd_solver_synchronize returns FDTD_ERR_DEVICE_TIMEOUT (once).  The
+ * fields of that step are not valid afterwards; the device context is. */
+int fdtd_solver_test_stall(fdtd_solver *s);
+
 /* Copies the current value of one field (after the last enqueued step) into
  * host memory (nx*ny*nz floats); synchronises the solver first. */
 int fdtd_solver_get_field(fdtd_solver *s, int field, float *host_out);
