@@ -53,14 +53,18 @@ __device__ __forceinline__ unsigned long long globaltimer_ns()
     return t;
 }
 
-// Bounded wait: false after MBAR_WAIT_NS of the global timer (read every
-// 256 polls once the first poll failed) or MBAR_SPIN_LIMIT polls.
+// Bounded wait: false after MBAR_SPIN_LIMIT polls or, once 16384 polls
+// failed, after MBAR_WAIT_NS of the global timer (read every 256 polls).  The
+// first polls read no timer: with the timer read after the first failed poll
+// both step kernels ran 0.7-1.1 % slower.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
 {
-    if (mbar_try_wait(bar, parity))
-        return true;
+    constexpr int FAST_POLLS = 16384;
+    for (int i = 0; i < FAST_POLLS; i++)
+        if (mbar_try_wait(bar, parity))
+            return true;
     const unsigned long long t0 = globaltimer_ns();
-    for (int i = 1; i < MBAR_SPIN_LIMIT; i++) {
+    for (int i = FAST_POLLS; i < MBAR_SPIN_LIMIT; i++) {
         if (mbar_try_wait(bar, parity))
             return true;
         if ((i & 255) == 0 && globaltimer_ns() - t0 > MBAR_WAIT_NS)
