@@ -70,6 +70,8 @@ def parse_args():
                     help="phantom: the 512x512x400 solve (default); batch: 64 uneven solves in one batch; "
                          "serve: a Poisson request stream through the serving loop")
     ap.add_argument("--batch-solves", type=int, default=64, help="solves of the batch workload (the first N)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="batch workload: choose the z-blocking depth with fdtd_batch_autotune before timing")
     ap.add_argument("--batch-steps", type=int, default=0,
                     help="timed steps of the batch workload (0: until the last solve ends)")
     ap.add_argument("--serve-rate", type=float, default=2.0, help="requests per second (serve)")
@@ -413,37 +415,43 @@ def run_batch_workload(args) -> None:
     warm = max(3, args.warmup)
     b.run(warm)
     b.synchronize()
+    zchunk = b.autotune() if args.autotune else 0  # its trial steps are real steps, before the timed region
+    pre = [b.steps(i) for i in ids]
     stream = torch.cuda.ExternalStream(b.stream)
     a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    longest = max(r.steps for r in reqs)
+    to_run = max(r.steps - d for r, d in zip(reqs, pre))
     if args.batch_steps > 0:
-        longest = min(longest, warm + args.batch_steps)
+        to_run = min(to_run, args.batch_steps)
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         a.record(stream)
-        b.run(longest - warm)
+        b.run(to_run)
         e.record(stream)
         b.synchronize()
         torch.cuda.synchronize()
     seconds = a.elapsed_time(e) / 1e3
-    assert all(b.steps(i) == min(r.steps, longest) for i, r in zip(ids, reqs))
+    post = [b.steps(i) for i in ids]
+    assert all(q == min(r.steps, d + to_run) for q, d, r in zip(post, pre, reqs))
     cells = [r.dims[0] * r.dims[1] * r.dims[2] for r in reqs]
-    updates = sum(c * (min(r.steps, longest) - warm) for c, r in zip(cells, reqs))
+    updates = sum(c * (q - d) for c, q, d in zip(cells, post, pre))
     peak, peak_kind = measured_peak_gbs()
     batch_b = FORM_BYTES["compact" if args.kernel == "compact" else "single"]
     line = {
         "metric": METRIC, "value": updates / seconds, "unit": "cell-updates/s", "n_gpus": 1,
-        "steps": longest - warm, "warmup": warm, "ms_per_step": seconds / (longest - warm) * 1e3,
+        "steps": to_run, "warmup": warm, "ms_per_step": seconds / to_run * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"batch of {len(reqs)} solves, dims log-uniform 48-256 per axis, 1-4 Debye ellipsoids, "
                                f"source U[0.3,3] GHz, steps U[500,3000], corrected scheme, {form_name(args)}",
                    "solves": len(reqs), "cells_total": sum(cells), "state_bytes": b.bytes,
-                   "cell_updates": updates, "l2": "state >> 129 MB L2: no flush"},
+                   "cell_updates": updates, "l2": "state >> 129 MB L2: no flush",
+                   "z_chunk_limit": zchunk or "default (compact 16, D form 64 planes)",
+                   "autotune": "fdtd_batch_autotune before timing (its trial steps are excluded)"
+                               if args.autotune else "off"},
         "roofline": {"bound": "hbm", "kernel": "batch step (all kernels)",
                      "achieved": batch_b * updates / seconds / 1e9, "peak": peak, "unit": "GB/s",
                      "frac": batch_b * updates / seconds / 1e9 / peak, "peak_kind": peak_kind, "traffic": None,
                      "algorithmic_bytes_per_cell_update": batch_b},
-        "gpu_launches": 3 * (longest - warm), "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
+        "gpu_launches": 3 * to_run, "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
     }
     b.close()
     tmp.cleanup()

@@ -169,6 +169,7 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_batch_remove", _I, _V, _I)
         _sig(L, "fdtd_batch_run", _I, _V, _I)
         _sig(L, "fdtd_batch_synchronize", _I, _V)
+        _sig(L, "fdtd_batch_autotune", _I, _V, _I, C.POINTER(_I))
         _sig(L, "fdtd_batch_steps", _I, _V, _I)
         _sig(L, "fdtd_batch_get_field", _I, _V, _I, _I, _I, _I, _P)
         _sig(L, "fdtd_batch_bytes", C.c_size_t, _V)
@@ -489,6 +490,13 @@ class Batch:
 
     def synchronize(self) -> None:
         check(lib().fdtd_batch_synchronize(self.handle), "fdtd_batch_synchronize")
+
+    def autotune(self, steps_per_trial: int = 16) -> int:
+        """Times each candidate z-chunk limit on the current solves (the trial
+        steps are real steps) and keeps the fastest; returns it (0: default)."""
+        chosen = C.c_int(0)
+        check(lib().fdtd_batch_autotune(self.handle, steps_per_trial, C.byref(chosen)), "fdtd_batch_autotune")
+        return chosen.value
 
     def steps(self, sid: int) -> int:
         return lib().fdtd_batch_steps(self.handle, sid)

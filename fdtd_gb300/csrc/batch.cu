@@ -72,6 +72,7 @@ struct fdtd_batch {
     BatchLaunch launch{};
     std::map<int, cudaGraphExec_t> graphs;  // steps per graph -> exec
     size_t bytes = 0;
+    int zchunk_max = 0;  // largest z chunk (fdtd_batch_autotune); 0: the form's default
 };
 
 namespace {
@@ -126,7 +127,8 @@ int rebuild(fdtd_batch *b)
             if (!encode_step_maps(d.c[par], b->compact, &d.maps[par]))
                 return FDTD_ERR_INVALID;
         }
-        d.zchunk = b->compact ? compact_zchunk(v->nz) : fused_zchunk(v->nz);
+        d.zchunk = b->zchunk_max > 0 ? zchunk_limited(v->nz, b->zchunk_max)
+                                     : (b->compact ? compact_zchunk(v->nz) : fused_zchunk(v->nz));
         d.tiles_x = (v->nx + 31) / 32;
         d.tiles_y = (v->ny + ty - 1) / ty;
         d.chunks = (v->nz + d.zchunk - 1) / d.zchunk;
@@ -201,6 +203,21 @@ int graph_for(fdtd_batch *b, int len, cudaGraphExec_t *out)
     b->graphs[len] = exec;
     *out = exec;
     return FDTD_OK;
+}
+
+// Sum over the solves of cells x completed steps (synchronises).
+int cell_steps(fdtd_batch *b, double *out)
+{
+    int st = cu(cudaStreamSynchronize(b->stream));
+    double sum = 0.0;
+    for (auto *v : b->solves) {
+        int n = 0;
+        if (st == FDTD_OK)
+            st = cu(cudaMemcpy(&n, v->counter, sizeof n, cudaMemcpyDeviceToHost));
+        sum += (double)v->nx * v->ny * v->nz * n;
+    }
+    *out = sum;
+    return st;
 }
 
 BatchSolve *find(fdtd_batch *b, int id)
@@ -379,6 +396,64 @@ int fdtd_batch_run(fdtd_batch *b, int nsteps)
             st = cu(cudaGraphLaunch(g, b->stream));
         nsteps -= len;
     }
+    return st;
+}
+
+int fdtd_batch_autotune(fdtd_batch *b, int steps_per_trial, int *chosen)
+{
+    if (!b || steps_per_trial < 1)
+        return FDTD_ERR_INVALID;
+    int st = cu(cudaSetDevice(b->device));
+    if (st != FDTD_OK)
+        return st;
+    // D form: at most 64 planes (the per-thread source-plane mask covers 66)
+    static const int compact_cands[] = {8, 12, 16, 24, 32, 48, 64};
+    static const int dform_cands[] = {16, 24, 32, 48, 64};
+    const int *cands = b->compact ? compact_cands : dform_cands;
+    const int ncand = b->compact ? 7 : 5;
+    const int trial = (steps_per_trial + 7) / 8 * 8;  // whole 8-step graphs only
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    st = cu(cudaEventCreate(&e0));
+    if (st == FDTD_OK)
+        st = cu(cudaEventCreate(&e1));
+    double best_cost = 0.0;
+    int best = 0;
+    for (int k = 0; k < ncand && st == FDTD_OK && !b->solves.empty(); k++) {
+        b->zchunk_max = cands[k];
+        b->dirty = true;
+        st = fdtd_batch_run(b, 8);  // rebuild and graph capture, untimed
+        double c0 = 0.0, c1 = 0.0;
+        if (st == FDTD_OK)
+            st = cell_steps(b, &c0);
+        if (st == FDTD_OK)
+            st = cu(cudaEventRecord(e0, b->stream));
+        if (st == FDTD_OK)
+            st = fdtd_batch_run(b, trial);
+        if (st == FDTD_OK)
+            st = cu(cudaEventRecord(e1, b->stream));
+        if (st == FDTD_OK)
+            st = cell_steps(b, &c1);
+        float ms = 0.0f;
+        if (st == FDTD_OK)
+            st = cu(cudaEventElapsedTime(&ms, e0, e1));
+        if (st == FDTD_OK && c1 > c0) {
+            const double cost = ms / (c1 - c0);
+            if (best == 0 || cost < best_cost) {
+                best_cost = cost;
+                best = cands[k];
+            }
+        }
+    }
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    b->zchunk_max = best;  // 0 when no trial advanced a solve: the default
+    b->dirty = true;
+    if (chosen)
+        *chosen = best;
+    if (st == FDTD_OK)
+        st = fdtd_batch_synchronize(b);
     return st;
 }
 

@@ -147,6 +147,7 @@ bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps);
 int fused_tile_height();
 int fused_zchunk(int nz);
 int compact_zchunk(int nz);
+int zchunk_limited(int nz, int max_planes);  // nz in equal chunks of at most max_planes planes
 // One batched step: fused kernel over all units, Mur faces, step counters.
 int launch_batch_step(const BatchLaunch &b, cudaStream_t s);
 int batch_persistent_ctas(bool compact, int nclasses);

@@ -723,7 +723,7 @@ int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 }  // namespace
 
 // nz split into equal chunks of at most max_planes planes
-static int zchunk_of(int nz, int max_planes)
+int zchunk_limited(int nz, int max_planes)
 {
     const int chunks = (nz + max_planes - 1) / max_planes;
     return (nz + chunks - 1) / chunks;
@@ -739,10 +739,10 @@ int fused_zchunk(int nz)
     // about 64 planes per CTA: enough CTAs per wave on 152 SMs, little
     // prologue/epilogue traffic at chunk borders.  At most 64: a unit's
     // per-thread source mask covers 66 planes.
-    return zchunk_of(nz, FDTD_ZCHUNK);
+    return zchunk_limited(nz, FDTD_ZCHUNK);
 }
 
-int compact_zchunk(int nz) { return zchunk_of(nz, FDTD_COMPACT_ZCHUNK); }
+int compact_zchunk(int nz) { return zchunk_limited(nz, FDTD_COMPACT_ZCHUNK); }
 
 bool fused_uses_tma(const NativeConsts &c)
 {

@@ -445,6 +445,15 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
 int fdtd_batch_remove(fdtd_batch *b, int id);
 /* Enqueues nsteps batched steps (asynchronous). */
 int fdtd_batch_run(fdtd_batch *b, int nsteps);
+/* Chooses the z-blocking depth of the batched kernel for the current solves
+ * (no counterpart in the reference): times steps_per_trial steps (rounded up
+ * to a multiple of 8, after 8 untimed steps) at each candidate largest z
+ * chunk (compact form 8-64 planes, D form 16-64) and keeps the one with the
+ * least time per cell-update.  The trial steps are real steps of the solves
+ * (a cell's update does not depend on where chunks meet, so the results are
+ * the same bits).  *chosen (optional): the chunk limit kept, 0 if no trial
+ * advanced a solve (the form's default stays).  Synchronises. */
+int fdtd_batch_autotune(fdtd_batch *b, int steps_per_trial, int *chosen);
 int fdtd_batch_synchronize(fdtd_batch *b);
 /* Completed steps of one solve (synchronises; -1 on error). */
 int fdtd_batch_steps(fdtd_batch *b, int id);

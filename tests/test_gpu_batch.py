@@ -108,3 +108,31 @@ def test_compact_batch_matches_lone_compact_solves_and_oracle(cuda):
             assert np.array_equal(got[name].view(np.uint32), alone[name].view(np.uint32)), (dims, name)
         assert_fields_close(got, _oracle(*case), names=list(got))
     b.close()
+
+
+@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT])
+def test_autotuned_batch_gives_the_same_bits(cuda, kernel):
+    """fdtd_batch_autotune times real steps of the solves at each candidate
+    z-chunk limit and keeps the fastest.  A cell's update does not depend on
+    where chunks meet, so every solve still equals the same solve run alone,
+    bit for bit, and the steps taken while tuning count."""
+    steps = 150  # outlasts the trials (at most 7 candidates x 16 steps)
+    b = fg.Batch(kernel=kernel)
+    cases = [_case(k) for k in range(len(CASES))]
+    ids = [b.add(Params(c[8]), c[3], c[4], steps, scheme=c[2]) for c in cases]
+    chosen = b.autotune(steps_per_trial=8)
+    cands = (8, 12, 16, 24, 32, 48, 64) if kernel == fg.KERNEL_COMPACT else (16, 24, 32, 48, 64)
+    assert chosen in cands
+    done = b.steps(ids[0])
+    assert 16 * len(cands) - 8 <= done <= 16 * len(cands), done
+    b.run(steps - done)
+    for sid, case in zip(ids, cases):
+        dims, _, scheme, codes, specs, sources, consts, jz, raw = case
+        assert b.steps(sid) == steps
+        got = b.fields(sid)
+        with fg.Solver(Params(raw), codes, specs, scheme=scheme, kernel=kernel) as s:
+            s.run(steps)
+            alone = s.fields()
+        for name in got:
+            assert np.array_equal(got[name].view(np.uint32), alone[name].view(np.uint32)), (dims, name)
+    b.close()
