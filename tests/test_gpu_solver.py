@@ -161,3 +161,37 @@ def test_binary_snapshots_hold_the_exact_fields(cuda, tmp_path):
         assert text == "".join("".join(" % 9.3E" % float(v) for v in row) + "\n" for row in raw[2])
     assert len(list(out.glob("*.f32"))) == 3 * 3
     assert len(list(out.glob("*.out"))) == 3 * 3 * 4
+
+
+def test_drop_in_voxel_cache_and_compact_binary_output(cuda, tmp_path):
+    """The drop-in with --voxel-cache: the first run parses the slices and
+    writes the cache, the second reads it; with --kernel compact --format
+    binary --fields ez both runs write the same Ez bits, equal to the
+    compact solver's."""
+    import subprocess
+
+    n = 16
+    path = ph.c1_inputs(tmp_path, n=n, t_max=6)
+    cache = tmp_path / "voxels.u8v"
+    runs = []
+    for k in range(2):
+        out = tmp_path / "out"
+        if out.exists():
+            for q in out.iterdir():
+                q.unlink()
+        else:
+            out.mkdir()
+        r = subprocess.run([str(fg.EXE_PATH), "--params", str(path), "--specs", str(tmp_path / "mat_specs"),
+                            "--kernel", "compact", "--format", "binary", "--fields", "ez",
+                            "--voxel-cache", str(cache)], capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert ("voxels from cache" if k else "voxel cache written") in r.stdout, r.stdout
+        files = sorted(out.glob("*.f32"))
+        assert len(files) == 6 and not list(out.glob("*.out"))
+        runs.append(np.fromfile(out / f"E_field_z_00005_z00000_n{n:05d}.f32", dtype="<f4").reshape(n, n, n))
+    assert np.array_equal(runs[0].view(np.uint32), runs[1].view(np.uint32))
+    p, codes, specs, s = solver_from_files(tmp_path / "again", n, 6, fg.KERNEL_COMPACT)
+    s.run(6)
+    ez = s.field("ez")
+    s.close()
+    assert np.array_equal(runs[1].view(np.uint32), ez.view(np.uint32))
