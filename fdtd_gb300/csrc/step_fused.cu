@@ -1,14 +1,17 @@
 // step_fused.cu -- the single-pass step: H, D, sources and the Debye E update
-// of one Yee step in one z-marching kernel, followed by the Mur face kernel.
+// of one Yee step in one z-marching kernel (with the x-face Mur updates),
+// followed by the Mur kernel for the y and z faces.
 //
 // Each CTA owns a 32 x TY column tile of (x, y) and a chunk of z planes.  Per
 // plane it stages, in shared memory, E^n with a one-cell halo on every side,
 // H^{n-1/2} with a one-cell halo at low x and low y, and the tile's D^n,
-// D^{n-1}, E^{n-1} and material classes.  It recomputes H^{n+1/2} on its low
-// halo, so that D^{n+1} = D^n + dt curl H^{n+1/2} needs no neighbour tile's
-// output; H is double-buffered (read H_old, write H_new), E and D are updated
-// in their "prev" slots.  Every array is therefore read once and written once
-// per step: 15 floats + 1 byte read, 9 floats written, 97 bytes per cell.
+// D^{n-1}, E^{n-1} (D form) or R (compact form) and material classes.  It
+// recomputes H^{n+1/2} on its low halo, so that D^{n+1} = D^n + dt curl
+// H^{n+1/2} needs no neighbour tile's output; H is double-buffered (read
+// H_old, write H_new), E and D are updated in their "prev" slots, R in place.
+// Every array is therefore read once and written once per step: 97 bytes per
+// cell in the D form (15 floats + 1 byte read, 9 floats written), 73 in the
+// compact form (9 + 1 byte read, 9 written).
 //
 // Staging: with nx a multiple of 16 and 16-byte aligned buffers, one thread
 // issues TMA tile loads (cp.async.bulk.tensor.3d) for a whole plane into an
@@ -16,10 +19,10 @@
 // raises the plan's error flag and the CTA stops).  Otherwise the same ring is
 // filled with 4-byte cp.async copies (zero-filled outside the grid).
 //
-// Shape (32 x 8 tiles, 3 stages, one issuing thread, Mur in its own kernel)
-// is the fastest of the variants measured on the 512 x 512 x 400 phantom:
-// 16-row tiles with 2 stages, 4 stages, Mur faces inside this kernel, and TMA
-// boxes issued by 16 lanes were each slower on the same GPU.
+// Shape (32 x 8 tiles, 3 stages, one issuing thread) is the fastest of the
+// variants measured on the 512 x 512 x 400 phantom: 16-row tiles with 2
+// stages, 4 stages, all Mur faces inside this kernel, and TMA boxes issued by
+// 16 lanes were each slower on the same GPU.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
