@@ -76,6 +76,10 @@ def parse_args():
                     help="timed steps of the batch workload (0: until the last solve ends)")
     ap.add_argument("--serve-rate", type=float, default=2.0, help="requests per second (serve)")
     ap.add_argument("--serve-seconds", type=float, default=60.0, help="length of the arrival window (serve)")
+    ap.add_argument("--serve-policy", choices=["fifo", "sjf"], default="fifo",
+                    help="admission order (serve): arrival order or shortest job first")
+    ap.add_argument("--serve-max-cells", type=float, default=0.0,
+                    help="cap on the cells of the admitted solves (serve; 0: memory budget only)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
     return ap.parse_args()
 
@@ -473,7 +477,8 @@ def run_serve_workload(args) -> None:
     with ClockSampler(0) as clk:
         res = sv.serve(reqs, budget_bytes=150 * 10 ** 9, chunk=25, snapshot_every=250, scheme=fg.SCHEME_CORRECTED,
                        inputs=inputs, on_snapshot=lambda r, step, plane: snaps.append(plane.nbytes),
-                       kernel=fg.KERNEL_COMPACT if args.kernel == "compact" else fg.KERNEL_SINGLE_PASS)
+                       kernel=fg.KERNEL_COMPACT if args.kernel == "compact" else fg.KERNEL_SINGLE_PASS,
+                       policy=args.serve_policy, max_active_cells=args.serve_max_cells or None)
     summ = res.summary()
     line = {
         "metric": "served cell-updates/s and latency", "value": summ["cell_updates_per_s"],
@@ -481,7 +486,9 @@ def run_serve_workload(args) -> None:
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"Poisson stream {args.serve_rate} req/s for {args.serve_seconds} s, dims "
                                f"log-uniform 64-384, steps U[500,4000], 150 GB budget, Ez snapshot every 250 "
-                               f"steps, corrected scheme, {form_name(args)}", "requests": len(reqs)},
+                               f"steps, corrected scheme, {form_name(args)}", "requests": len(reqs),
+                   "policy": args.serve_policy,
+                   "max_active_cells": args.serve_max_cells or "memory budget only"},
         "serve": {**summ, "snapshot_bytes": int(sum(snaps)), "snapshots": len(snaps)},
         "clocks": clk.summary(),
     }

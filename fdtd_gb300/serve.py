@@ -2,7 +2,8 @@
 
 Requests (grid, seeded phantom, source frequency, step count) arrive as a
 Poisson stream.  Between chunks of batched steps the loop admits queued
-requests in arrival order while their device state fits the memory budget,
+requests (in arrival order, or shortest job first) while their device state
+fits the memory budget and, optionally, their cells fit a cap,
 streams a snapshot (the Ez plane through the source) of every solve whose step
 count reached a multiple of the snapshot period, and retires finished solves,
 freeing their memory for the queue.  Work of all admitted solves overlaps on
@@ -96,28 +97,51 @@ class ServeResult:
                 "wall_s": self.wall}
 
 
+def work(req: Request) -> float:
+    """Cell-updates of a request."""
+    return float(req.dims[0]) * req.dims[1] * req.dims[2] * req.steps
+
+
+def order_queue(queue: list[Request], policy: str) -> None:
+    """Admission order, in place: "fifo" keeps arrival order, "sjf" puts the
+    request with the least work first (ties by arrival)."""
+    if policy == "sjf":
+        queue.sort(key=lambda r: (work(r), r.arrival))
+    elif policy != "fifo":
+        raise ValueError(f"unknown policy {policy!r}")
+
+
 def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_every: int = 250,
           scheme: int = SCHEME_CORRECTED, device: int = 0, clock=time.perf_counter,
-          on_snapshot=None, inputs: dict | None = None, kernel: int = KERNEL_SINGLE_PASS) -> ServeResult:
+          on_snapshot=None, inputs: dict | None = None, kernel: int = KERNEL_SINGLE_PASS,
+          policy: str = "fifo", max_active_cells: float | None = None) -> ServeResult:
     """Runs the request stream to completion in real time.  chunk must
     divide snapshot_every so snapshots land on exact step counts.  inputs
     (optional) maps request ids to build_inputs results that arrive with the
     requests; missing ones are built at admission.  kernel selects the state
-    form of every solve (KERNEL_SINGLE_PASS or KERNEL_COMPACT)."""
+    form of every solve (KERNEL_SINGLE_PASS or KERNEL_COMPACT).  policy: the
+    admission order ("fifo" or "sjf", see order_queue).  max_active_cells
+    (optional) caps the cells of the admitted solves: the batched launch
+    needs only enough of them to fill the GPU, and admitting more only shares
+    it among more requests, which lengthens every one; a request is admitted
+    alone when nothing runs, whatever its size."""
     assert snapshot_every % chunk == 0
+    order_queue([], policy)  # rejects an unknown policy before any work
     pending = sorted(requests, key=lambda r: r.arrival)
     queue: list[Request] = []
     active: dict[int, tuple[Request, int, int, Params]] = {}  # sid -> (req, steps done, snapshot z, params)
     batch = Batch(device, kernel)
     tmp = tempfile.TemporaryDirectory()
     cell_updates = 0.0
+    active_cells = 0.0
     t0 = clock()
     try:
         while pending or queue or active:
             now = clock() - t0
             while pending and pending[0].arrival <= now:
                 queue.append(pending.pop(0))
-            # admit in arrival order while the head fits the budget
+            # admit in policy order while the head fits the budget and the cap
+            order_queue(queue, policy)
             while queue:
                 req = queue[0]
                 need = batch.need_bytes(*req.dims)
@@ -125,6 +149,9 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
                     queue.pop(0)  # can never fit: drop (done stays NaN)
                     continue
                 if batch.bytes + need > budget_bytes:
+                    break
+                cells = float(req.dims[0]) * req.dims[1] * req.dims[2]
+                if max_active_cells is not None and active and active_cells + cells > max_active_cells:
                     break
                 queue.pop(0)
                 if inputs is not None and req.rid in inputs:
@@ -134,6 +161,7 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
                 sid = batch.add(p, codes, specs, req.steps, scheme=scheme)
                 req.admitted = clock() - t0
                 active[sid] = (req, 0, src[2], p)
+                active_cells += cells
             if not active:
                 if pending:  # idle until the next arrival
                     time.sleep(max(0.0, min(0.05, pending[0].arrival - (clock() - t0))))
@@ -155,6 +183,7 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
                     finished.append(sid)
             for sid in finished:
                 req = active.pop(sid)[0]
+                active_cells -= float(req.dims[0]) * req.dims[1] * req.dims[2]
                 req.done = clock() - t0
                 if on_snapshot is not None and hasattr(on_snapshot, "final"):
                     on_snapshot.final(req, batch, sid)

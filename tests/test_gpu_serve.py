@@ -23,15 +23,19 @@ class Recorder:
         self.finals[req.rid] = batch.fields(sid)
 
 
-@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT])
-def test_served_results_equal_lone_runs_and_overlap(cuda, tmp_path, kernel):
+@pytest.mark.parametrize("kernel,policy", [(fg.KERNEL_SINGLE_PASS, "fifo"), (fg.KERNEL_COMPACT, "fifo"),
+                                           (fg.KERNEL_COMPACT, "sjf")])
+def test_served_results_equal_lone_runs_and_overlap(cuda, tmp_path, kernel, policy):
     reqs = serve.poisson_stream(rate=40.0, duration=0.3, seed=3, dims=(24, 56), steps=(50, 150))
     assert len(reqs) >= 4
     for r in reqs:  # whole chunks keep the snapshot steps exact
         r.steps = (r.steps // 25) * 25 or 25
     rec = Recorder()
     budget = sum(fg.Batch.solve_bytes(*r.dims) for r in reqs[:3])  # forces queueing
-    res = serve.serve(reqs, budget_bytes=budget, chunk=25, snapshot_every=50, on_snapshot=rec, kernel=kernel)
+    # sjf: also a cell cap that holds about two of these solves at a time
+    cap = 2.0 * 40 ** 3 if policy == "sjf" else None
+    res = serve.serve(reqs, budget_bytes=budget, chunk=25, snapshot_every=50, on_snapshot=rec, kernel=kernel,
+                      policy=policy, max_active_cells=cap)
     s = res.summary()
     assert s["completed"] == len(reqs)
     # continuous batching: some request was admitted while another was still running
