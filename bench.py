@@ -43,14 +43,23 @@ B_ALG = 97  # bytes per cell-update: 15 state floats read, 9 written, 1-byte cla
 KERNEL_BYTES = {
     "fused_step": 97,    # H, E^n, E^{n-1}, D^n, D^{n-1} read; H, E, D written; class
     "compact_step": 73,  # H, E^n, R read; H, E, R written; class
+    # H, E^n read and written as floats, R as int16, one 4-byte exponent word per 32 cells, class
+    "compact16_step": 61.25,
     "de": 85,            # H, E^n, E^{n-1}, D^n, D^{n-1} read; E, D written; class
     "h": 36,             # H, E read; H written
 }
-KERNELS = {"single": 0, "two_pass": 1, "compact": 2}
+KERNELS = {"single": 0, "two_pass": 1, "compact": 2, "compact16": 3}
 # algorithmic bytes per cell-update of a whole step of each state form
-FORM_BYTES = {"single": B_ALG, "two_pass": B_ALG, "compact": 73}
+FORM_BYTES = {"single": B_ALG, "two_pass": B_ALG, "compact": 73, "compact16": 61.25}
 # resident bytes per cell (H double-buffered for the single-pass kernels)
-STATE_BYTES = {"single": 73, "two_pass": 61, "compact": 61}
+STATE_BYTES = {"single": 73, "two_pass": 61, "compact": 61, "compact16": 55.125}
+FORM_STATE = {
+    "compact": "H (2 buffers), E (2 slots), R = -a E^{n-1} - 2 tau (D^n - D^{n-1}); D not stored",
+    "compact16": "as compact, R stored as int16 with one exponent byte per component per 32-cell row segment "
+                 "(15 significant bits for the segment's largest value); FP32 arithmetic; D not stored",
+}
+PRECISION_PROBES = 16
+PRECISION_SEED = 2024
 METRIC = "cell-updates/s"
 
 
@@ -81,6 +90,9 @@ def parse_args():
     ap.add_argument("--serve-max-cells", type=float, default=0.0,
                     help="cap on the cells of the admitted solves (serve; 0: memory budget only)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
+    ap.add_argument("--no-precision", action="store_true",
+                    help="skip the probe/DFT/SAR error of the 16-bit-R form against the D form")
+    ap.add_argument("--precision-steps", type=int, default=3000, help="steps of the precision comparison")
     return ap.parse_args()
 
 
@@ -240,6 +252,62 @@ def run_reference_arm(args, rank: int, world: int) -> None:
     print(json.dumps(line), flush=True)
 
 
+def precision_probes(codes: np.ndarray, n: int = PRECISION_PROBES, seed: int = PRECISION_SEED):
+    """n seeded cells drawn uniformly from the phantom's tissue (class > 0),
+    at least 2 cells from every face; (x, y, z) tuples."""
+    nz, ny, nx = codes.shape
+    inner = np.zeros(codes.shape, bool)
+    inner[2:nz - 2, 2:ny - 2, 2:nx - 2] = True
+    cand = np.flatnonzero((codes > 0) & inner)
+    pick = np.random.default_rng(seed).choice(cand, size=n, replace=False)
+    z, rem = np.divmod(pick, ny * nx)
+    y, x = np.divmod(rem, nx)
+    return [(int(a), int(b), int(c)) for a, b, c in zip(x, y, z)]
+
+
+def precision_check(p, codes, specs, dev: int, steps: int) -> dict:
+    """Error of the 16-bit-R compact form (and of the 32-bit compact form)
+    against the D form, all on the GPU, corrected scheme, `steps` steps:
+    E series at 16 seeded probe points inside the phantom (relative L2 per
+    probe over the 3 components and all steps), the running DFT |E| at the
+    source's 900 MHz over 32 planes through the source, and the peak
+    spectral SAR over those planes.  The D form itself is held to the FP64
+    oracle by the parity tests (grids the oracle runs in seconds)."""
+    import fdtd_gb300 as fg
+
+    nz = codes.shape[0]
+    probes = precision_probes(codes)
+    freq = float(p.wave_frequency) * float(p.pulse_modulation_frequency)
+    z0, nplanes = max(0, nz // 2 - 16), min(32, nz)
+
+    def run(kernel):
+        s = fg.Solver(p, codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel, device=dev)
+        s.set_probes(probes, capacity=steps)
+        s.set_dft(freq, stride=5, z0=z0, nplanes=nplanes)
+        s.run(steps)
+        s.synchronize()
+        series = s.probes().astype(np.float64)
+        e2 = None
+        for comp in range(3):
+            a = s.dft(comp)
+            e2 = np.abs(a) ** 2 if e2 is None else e2 + np.abs(a) ** 2
+        sar, cell = s.peak_sar()
+        s.close()
+        return series, np.sqrt(e2), sar, cell
+
+    ref = run(fg.KERNEL_SINGLE_PASS)
+    out = {"reference": "FP32 D form on the GPU (same workload, corrected scheme)", "steps": steps,
+           "probes": probes, "dft_hz": freq, "dft_planes": [z0, z0 + nplanes]}
+    for name, kernel in (("compact16", fg.KERNEL_COMPACT_R16), ("compact", fg.KERNEL_COMPACT)):
+        series, amp, sar, cell = run(kernel)
+        per = [float(np.linalg.norm(series[:, j] - ref[0][:, j]) / max(np.linalg.norm(ref[0][:, j]), 1e-300))
+               for j in range(len(probes))]
+        out[name] = {"probe_rel_l2_max": max(per), "probe_rel_l2_median": float(np.median(per)),
+                     "dft_abs_e_rel_l2": float(np.linalg.norm(amp - ref[1]) / np.linalg.norm(ref[1])),
+                     "peak_sar_rel": float(abs(sar - ref[2]) / ref[2]), "peak_sar_same_cell": cell == ref[3]}
+    return out
+
+
 def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
     import torch
 
@@ -276,37 +344,39 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
     kernels_per_step = len(prof)
     s.close()
 
-    # ---- the compact nine-field form on the same workload (reported beside
-    # the D form; same metric, same timing rules, its own clock record)
+    # ---- the compact forms on the same workload (reported beside the D
+    # form; same metric, same timing rules, their own clock records)
     forms = {}
     if args.kernel == "single" and not args.no_forms:
-        c = fg.Solver(p, codes, specs, scheme=scheme, kernel=KERNELS["compact"], device=local_rank)
-        cstream = torch.cuda.ExternalStream(c.stream)
-        c.run(args.warmup)
-        c.synchronize()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with ClockSampler(local_rank) as cclk:
-            replicas.barrier(dist)
-            torch.cuda.synchronize()
-            a.record(cstream)
-            c.run(args.steps)
-            b.record(cstream)
+        for fname in ("compact", "compact16"):
+            c = fg.Solver(p, codes, specs, scheme=scheme, kernel=KERNELS[fname], device=local_rank)
+            cstream = torch.cuda.ExternalStream(c.stream)
+            c.run(args.warmup)
             c.synchronize()
-            torch.cuda.synchronize()
-            replicas.barrier(dist)
-        c_cells, c_t = replicas.aggregate(cells * args.steps, a.elapsed_time(b) / 1e3, dist,
-                                          device=f"cuda:{local_rank}")
-        cprof = c.profile(min(args.steps, 20))
-        c.close()
-        cmain = max(cprof, key=cprof.get)
-        forms["compact"] = {
-            "value": c_cells / c_t, "unit": "cell-updates/s", "ms_per_step": c_t / args.steps * 1e3,
-            "state": "H (2 buffers), E (2 slots), R = -a E^{n-1} - 2 tau (D^n - D^{n-1}); D not stored",
-            "b_alg_bytes_per_cell_update": FORM_BYTES["compact"], "kernel_ms": cprof,
-            "roofline_kernel": cmain,
-            "roofline_achieved_gbs": KERNEL_BYTES.get(cmain, 0) * cells / (cprof[cmain] / 1e3) / 1e9,
-            "roofline_traffic": committed_traffic(cmain, cells),
-            "gpu_launches": len(cprof) * args.steps, "clocks": cclk.summary()}
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with ClockSampler(local_rank) as cclk:
+                replicas.barrier(dist)
+                torch.cuda.synchronize()
+                a.record(cstream)
+                c.run(args.steps)
+                b.record(cstream)
+                c.synchronize()
+                torch.cuda.synchronize()
+                replicas.barrier(dist)
+            c_cells, c_t = replicas.aggregate(cells * args.steps, a.elapsed_time(b) / 1e3, dist,
+                                              device=f"cuda:{local_rank}")
+            cprof = c.profile(min(args.steps, 20))
+            c.close()
+            cmain = max(cprof, key=cprof.get)
+            forms[fname] = {
+                "value": c_cells / c_t, "unit": "cell-updates/s", "ms_per_step": c_t / args.steps * 1e3,
+                "state": FORM_STATE[fname], "b_alg_bytes_per_cell_update": FORM_BYTES[fname], "kernel_ms": cprof,
+                "roofline_kernel": cmain,
+                "roofline_achieved_gbs": KERNEL_BYTES.get(cmain, 0) * cells / (cprof[cmain] / 1e3) / 1e9,
+                "roofline_traffic": committed_traffic(cmain, cells),
+                "gpu_launches": len(cprof) * args.steps, "clocks": cclk.summary()}
+        if not args.no_precision:
+            forms["compact16"]["precision"] = precision_check(p, codes, specs, local_rank, args.precision_steps)
 
     # ---- end to end through the C ABI with host buffers (e2e)
     e2e = None
@@ -376,7 +446,8 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
 # ------------------------------------------------------- batched / served
 
 def form_name(args) -> str:
-    return "compact form (H, E, R)" if args.kernel == "compact" else "D form"
+    return {"compact": "compact form (H, E, R)", "compact16": "compact form with 16-bit R (H, E, R16)"}.get(
+        args.kernel, "D form")
 
 def _request_inputs(reqs, root: Path, threads: int = 8) -> dict:
     """Inputs of each request (input_params + mat_specs + class volume), built
@@ -439,7 +510,7 @@ def run_batch_workload(args) -> None:
     cells = [r.dims[0] * r.dims[1] * r.dims[2] for r in reqs]
     updates = sum(c * (q - d) for c, q, d in zip(cells, post, pre))
     peak, peak_kind = measured_peak_gbs()
-    batch_b = FORM_BYTES["compact" if args.kernel == "compact" else "single"]
+    batch_b = FORM_BYTES[args.kernel if args.kernel in ("compact", "compact16") else "single"]
     line = {
         "metric": METRIC, "value": updates / seconds, "unit": "cell-updates/s", "n_gpus": 1,
         "steps": to_run, "warmup": warm, "ms_per_step": seconds / to_run * 1e3,
@@ -477,7 +548,7 @@ def run_serve_workload(args) -> None:
     with ClockSampler(0) as clk:
         res = sv.serve(reqs, budget_bytes=150 * 10 ** 9, chunk=25, snapshot_every=250, scheme=fg.SCHEME_CORRECTED,
                        inputs=inputs, on_snapshot=lambda r, step, plane: snaps.append(plane.nbytes),
-                       kernel=fg.KERNEL_COMPACT if args.kernel == "compact" else fg.KERNEL_SINGLE_PASS,
+                       kernel=KERNELS[args.kernel] if args.kernel != "two_pass" else fg.KERNEL_SINGLE_PASS,
                        policy=args.serve_policy, max_active_cells=args.serve_max_cells or None)
     summ = res.summary()
     line = {

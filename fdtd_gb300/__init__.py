@@ -43,6 +43,8 @@ SCHEME_CORRECTED = 1
 KERNEL_SINGLE_PASS = 0
 KERNEL_TWO_PASS = 1
 KERNEL_COMPACT = 2      # nine stored fields (H, E, R); D is not readable
+KERNEL_COMPACT_R16 = 3  # the same with R in 16 bits (int16 + one exponent per 32-cell row segment)
+COMPACT_KERNELS = (KERNEL_COMPACT, KERNEL_COMPACT_R16)
 FIELDS = ("hx", "hy", "hz", "dx", "dy", "dz", "ex", "ey", "ez")
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}
 
@@ -356,7 +358,7 @@ class Solver:
 
     def fields(self) -> dict[str, np.ndarray]:
         """Every stored field (the compact form stores no D)."""
-        names = [n for n in FIELDS if not (self.kernel == KERNEL_COMPACT and n.startswith("d"))]
+        names = [n for n in FIELDS if not (self.kernel in COMPACT_KERNELS and n.startswith("d"))]
         return {n: self.field(n) for n in names}
 
     def set_snapshots(self, every: int, fields=("ex", "ey", "ez"), z0: int = 0, nplanes: int = 0,
@@ -451,7 +453,8 @@ class Batch:
     """Many independent solves advanced together (fdtd_batch_*)."""
 
     def __init__(self, device: int = 0, kernel: int = KERNEL_SINGLE_PASS):
-        """kernel: KERNEL_SINGLE_PASS (D form) or KERNEL_COMPACT for every solve."""
+        """kernel: KERNEL_SINGLE_PASS (D form), KERNEL_COMPACT or KERNEL_COMPACT_R16 for
+        every solve."""
         h = C.c_void_p()
         check(lib().fdtd_batch_create_form(device, kernel, C.byref(h)), "fdtd_batch_create_form")
         self.handle = h
@@ -509,7 +512,7 @@ class Batch:
         return out
 
     def fields(self, sid: int) -> dict[str, np.ndarray]:
-        names = [n for n in FIELDS if not (self.kernel == KERNEL_COMPACT and n.startswith("d"))]
+        names = [n for n in FIELDS if not (self.kernel in COMPACT_KERNELS and n.startswith("d"))]
         return {n: self.field(sid, n) for n in names}
 
     @property

@@ -1,7 +1,8 @@
 // batch.cu -- many independent solves of uneven sizes advanced together.
 //
 // Each solve keeps its own resident state (H x2, E x2, D x2 or, in a batch of
-// the compact form, R x1, and the classes) with
+// the compact form, R x1 -- int16 R and its exponent words in the 16-bit
+// form -- and the classes) with
 // rows padded to a multiple of 16 cells, so every solve gets TMA staging, and
 // its own plan (class table, source table, Mur slabs) and step counter.  A
 // batched step is three launches: one persistent kernel over the work units
@@ -36,16 +37,21 @@ struct BatchSolve {
     float *e[2][3] = {};
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
+    uint32_t *rexp = nullptr;  // 16-bit R form: exponent words
     int *counter = nullptr;
 };
 
 size_t padded_pitch(int nx) { return ((size_t)nx + 15) & ~size_t(15); }
 
-size_t state_bytes(int nx, int ny, int nz, bool compact)
+size_t r16_array_bytes(size_t ncell) { return (ncell * sizeof(int16_t) + 255) & ~size_t(255); }
+size_t r16_exp_bytes(int nx, int ny, int nz) { return (r16_words(nx, ny, nz) * sizeof(uint32_t) + 255) & ~size_t(255); }
+
+size_t state_bytes(int nx, int ny, int nz, bool compact, bool r16 = false)
 {
     const size_t ncell = padded_pitch(nx) * ny * nz;
     const size_t f = (ncell * sizeof(float) + 255) & ~size_t(255);
-    return (compact ? 15 : 18) * f + ((ncell + 255) & ~size_t(255)) + 256;
+    const size_t d = r16 ? 3 * r16_array_bytes(ncell) + r16_exp_bytes(nx, ny, nz) : (compact ? 3 : 6) * f;
+    return 12 * f + d + ((ncell + 255) & ~size_t(255)) + 256;
 }
 
 size_t plan_bytes(int nx, int ny, int nz)
@@ -60,6 +66,7 @@ size_t plan_bytes(int nx, int ny, int nz)
 struct fdtd_batch {
     int device = 0;
     bool compact = false;  // every solve keeps the compact state
+    bool r16 = false;      // ... with R in 16 bits
     cudaStream_t stream = nullptr;
     std::vector<BatchSolve *> solves;
     int next_id = 1;
@@ -109,6 +116,7 @@ NativeConsts solve_consts(const BatchSolve *v, int parity)
     NativeConsts c = make_consts(v->plan, &f, 0);
     c.pitch = v->pitch;
     c.step_counter = v->counter;
+    c.r_exp = v->rexp;
     return c;
 }
 
@@ -124,7 +132,7 @@ int rebuild(fdtd_batch *b)
         std::memset(&d, 0, sizeof d);
         for (int par = 0; par < 2; par++) {
             d.c[par] = solve_consts(v, par);
-            if (!encode_step_maps(d.c[par], b->compact, &d.maps[par]))
+            if (!encode_step_maps(d.c[par], b->compact, &d.maps[par], b->r16))
                 return FDTD_ERR_INVALID;
         }
         d.zchunk = b->zchunk_max > 0 ? zchunk_limited(v->nz, b->zchunk_max)
@@ -170,7 +178,8 @@ int rebuild(fdtd_batch *b)
     for (auto *v : b->solves)
         max_classes = std::max(max_classes, v->plan->nclasses);
     b->launch = BatchLaunch{b->d_descs, (int)descs.size(), units, b->d_work, b->d_mur, (int)mur.size(),
-                            batch_persistent_ctas(b->compact, max_classes), b->compact ? 1 : 0, max_classes};
+                            batch_persistent_ctas(b->compact, max_classes, b->r16), b->compact ? 1 : 0, max_classes,
+                            b->r16 ? 1 : 0};
     drop_graphs(b);
     b->dirty = false;
     return FDTD_OK;
@@ -243,14 +252,15 @@ size_t fdtd_batch_need_bytes(const fdtd_batch *b, int nx, int ny, int nz)
 {
     if (!b || nx < 3 || ny < 3 || nz < 3)
         return 0;
-    return state_bytes(nx, ny, nz, b->compact) + plan_bytes(nx, ny, nz);
+    return state_bytes(nx, ny, nz, b->compact, b->r16) + plan_bytes(nx, ny, nz);
 }
 
 int fdtd_batch_create(int device, fdtd_batch **out) { return fdtd_batch_create_form(device, FDTD_KERNEL_SINGLE_PASS, out); }
 
 int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out)
 {
-    if (!out || (kernel != FDTD_KERNEL_SINGLE_PASS && kernel != FDTD_KERNEL_COMPACT))
+    if (!out || (kernel != FDTD_KERNEL_SINGLE_PASS && kernel != FDTD_KERNEL_COMPACT &&
+                 kernel != FDTD_KERNEL_COMPACT_R16))
         return FDTD_ERR_INVALID;
     int st = cu(cudaSetDevice(device));
     if (st != FDTD_OK)
@@ -259,7 +269,8 @@ int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out)
     if (!b)
         return FDTD_ERR_NOMEM;
     b->device = device;
-    b->compact = kernel == FDTD_KERNEL_COMPACT;
+    b->compact = kernel == FDTD_KERNEL_COMPACT || kernel == FDTD_KERNEL_COMPACT_R16;
+    b->r16 = kernel == FDTD_KERNEL_COMPACT_R16;
     st = cu(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     if (st == FDTD_OK)
         st = cu(cudaMalloc(&b->d_work, 256));
@@ -320,7 +331,8 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
     v->steps_target = steps;
     st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &v->plan);
     const size_t fbytes = (v->ncell * sizeof(float) + 255) & ~size_t(255);
-    const size_t total = state_bytes(p->nx, p->ny, p->nz, b->compact);
+    const size_t total = state_bytes(p->nx, p->ny, p->nz, b->compact, b->r16);
+    const size_t dbytes = b->r16 ? r16_array_bytes(v->ncell) : fbytes;
     if (st == FDTD_OK)
         st = cu(cudaMalloc(&v->d_block, total));
     if (st == FDTD_OK)
@@ -335,11 +347,15 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
                 v->e[s][k] = reinterpret_cast<float *>(q);
         const int nd = b->compact ? 1 : 2;  // D^n, D^{n-1} slots, or the one R array
         for (int s = 0; s < nd; s++)
-            for (int k = 0; k < 3; k++, q += fbytes)
+            for (int k = 0; k < 3; k++, q += dbytes)
                 v->d[s][k] = reinterpret_cast<float *>(q);
         if (nd == 1)
             for (int k = 0; k < 3; k++)
                 v->d[1][k] = v->d[0][k];
+        if (b->r16) {
+            v->rexp = reinterpret_cast<uint32_t *>(q);
+            q += r16_exp_bytes(p->nx, p->ny, p->nz);
+        }
         v->mat = reinterpret_cast<uint8_t *>(q);
         q += (v->ncell + 255) & ~size_t(255);
         v->counter = reinterpret_cast<int *>(q);

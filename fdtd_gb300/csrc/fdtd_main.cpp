@@ -89,15 +89,16 @@ int main(int argc, char **argv)
         else if (a == "--timeskip") timeskip = std::strtof(next(), nullptr);
         else if (a == "--kernel") {
             const char *k = next();
-            kernel = std::strcmp(k, "two") == 0       ? FDTD_KERNEL_TWO_PASS
-                     : std::strcmp(k, "compact") == 0 ? FDTD_KERNEL_COMPACT
-                                                      : FDTD_KERNEL_SINGLE_PASS;
+            kernel = std::strcmp(k, "two") == 0         ? FDTD_KERNEL_TWO_PASS
+                     : std::strcmp(k, "compact") == 0   ? FDTD_KERNEL_COMPACT
+                     : std::strcmp(k, "compact16") == 0 ? FDTD_KERNEL_COMPACT_R16
+                                                        : FDTD_KERNEL_SINGLE_PASS;
         }
         else if (a == "--device") device = std::atoi(next());
         else if (a == "--voxel-cache") voxel_cache = next();
         else {
             std::fprintf(stderr, "usage: %s [--params P] [--specs P] [--scheme reference|corrected] [--every N] "
-                                 "[--fields hx,...] [--format text|binary|both] [--timeskip X] [--kernel single|two|compact] [--voxel-cache P] [--device N]\n", argv[0]);
+                                 "[--fields hx,...] [--format text|binary|both] [--timeskip X] [--kernel single|two|compact|compact16] [--voxel-cache P] [--device N]\n", argv[0]);
             return 2;
         }
     }
@@ -143,8 +144,8 @@ int main(int argc, char **argv)
     fdtd_solver *s = nullptr;
     if ((st = fdtd_solver_create(&cfg, &s)) != FDTD_OK)
         return fail("solver", st);
-    if (kernel == FDTD_KERNEL_COMPACT)
-        mask &= ~(7u << FDTD_FIELD_DX);  // the compact form stores no D
+    if (kernel == FDTD_KERNEL_COMPACT || kernel == FDTD_KERNEL_COMPACT_R16)
+        mask &= ~(7u << FDTD_FIELD_DX);  // the compact forms store no D
     if (every > 0 && mask) {
         fdtd_snapshot_spec spec{};
         spec.every = every;

@@ -320,23 +320,48 @@ struct CheckpointHeader {
 static const char CKP_MAGIC[8] = {'F', 'D', 'T', 'D', 'G', 'B', '3', 'C'};
 
 // Checkpoint versions: 1 holds the D form's 15 arrays (either D-form
-// kernel restores it), 2 the compact form's 12.
-static uint32_t ckp_version(const fdtd_solver *s) { return s->kernel == FDTD_KERNEL_COMPACT ? 2u : 1u; }
-static int ckp_arrays(const fdtd_solver *s) { return s->kernel == FDTD_KERNEL_COMPACT ? 12 : 15; }
+// kernel restores it), 2 the compact form's 12, 3 the 16-bit-R form's 9
+// float arrays, its three int16 R arrays and its exponent words.
+static uint32_t ckp_version(const fdtd_solver *s)
+{
+    return s->kernel == FDTD_KERNEL_COMPACT_R16 ? 3u : s->kernel == FDTD_KERNEL_COMPACT ? 2u : 1u;
+}
 
-// The state arrays after `count` steps: H, E^n, E^{n-1}, then D^n, D^{n-1}
-// (D form) or R (compact form).
-static void state_arrays(fdtd_solver *s, int count, float *out[15])
+// The state blocks after `count` steps: H, E^n, E^{n-1}, then D^n, D^{n-1}
+// (D form), R (compact form) or the int16 R and the exponent words.
+static int state_blocks(fdtd_solver *s, int count, void *ptr[16], size_t bytes[16])
 {
     const int hb = s->kernel != FDTD_KERNEL_TWO_PASS ? (count & 1) : 0;
     const int l = latest_slot(count), p = previous_slot(count);
+    const size_t fb = sizeof(float) * s->ncell;
+    int n = 0;
     for (int c = 0; c < 3; c++) {
-        out[c] = s->h[hb][c];
-        out[3 + c] = s->e[l][c];
-        out[6 + c] = s->e[p][c];
-        out[9 + c] = s->d[l][c];
-        out[12 + c] = s->d[p][c];
+        ptr[n] = s->h[hb][c];
+        ptr[n + 3] = s->e[l][c];
+        ptr[n + 6] = s->e[p][c];
+        bytes[n] = bytes[n + 3] = bytes[n + 6] = fb;
+        n++;
     }
+    n = 9;
+    if (s->kernel == FDTD_KERNEL_COMPACT_R16) {
+        for (int c = 0; c < 3; c++, n++) {
+            ptr[n] = s->d[0][c];
+            bytes[n] = sizeof(int16_t) * s->ncell;
+        }
+        ptr[n] = s->rexp;
+        bytes[n++] = sizeof(uint32_t) * r16_words(s->nx, s->ny, s->nz);
+        return n;
+    }
+    for (int c = 0; c < 3; c++, n++) {
+        ptr[n] = s->d[l][c];
+        bytes[n] = fb;
+    }
+    if (s->kernel != FDTD_KERNEL_COMPACT)
+        for (int c = 0; c < 3; c++, n++) {
+            ptr[n] = s->d[p][c];
+            bytes[n] = fb;
+        }
+    return n;
 }
 
 int fdtd_solver_checkpoint(fdtd_solver *s, const char *path)
@@ -358,12 +383,14 @@ int fdtd_solver_checkpoint(fdtd_solver *s, const char *path)
     h.steps = s->steps;
     h.material_hash = s->material_hash;
     bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
-    float *arrs[15];
-    state_arrays(s, s->steps, arrs);
-    std::vector<float> buf(s->ncell);
-    for (int k = 0; k < ckp_arrays(s) && ok; k++) {
-        st = cu(cudaMemcpy(buf.data(), arrs[k], sizeof(float) * s->ncell, cudaMemcpyDeviceToHost));
-        ok = st == FDTD_OK && std::fwrite(buf.data(), sizeof(float), s->ncell, f) == s->ncell;
+    void *ptr[16];
+    size_t bytes[16];
+    const int nb = state_blocks(s, s->steps, ptr, bytes);
+    std::vector<char> buf(sizeof(float) * s->ncell);
+    for (int k = 0; k < nb && ok; k++) {
+        buf.resize(bytes[k]);
+        st = cu(cudaMemcpy(buf.data(), ptr[k], bytes[k], cudaMemcpyDeviceToHost));
+        ok = st == FDTD_OK && std::fwrite(buf.data(), 1, bytes[k], f) == bytes[k];
     }
     if (std::fclose(f) != 0)
         ok = false;
@@ -391,14 +418,16 @@ int fdtd_solver_restore(fdtd_solver *s, const char *path)
         std::fclose(f);
         return FDTD_ERR_FORMAT;
     }
-    float *arrs[15];
-    state_arrays(s, h.steps, arrs);
-    std::vector<float> buf(s->ncell);
+    void *ptr[16];
+    size_t bytes[16];
+    const int nb = state_blocks(s, h.steps, ptr, bytes);
+    std::vector<char> buf;
     bool ok = true;
-    for (int k = 0; k < ckp_arrays(s) && ok && st == FDTD_OK; k++) {
-        ok = std::fread(buf.data(), sizeof(float), s->ncell, f) == s->ncell;
+    for (int k = 0; k < nb && ok && st == FDTD_OK; k++) {
+        buf.resize(bytes[k]);
+        ok = std::fread(buf.data(), 1, bytes[k], f) == bytes[k];
         if (ok)
-            st = cu(cudaMemcpy(arrs[k], buf.data(), sizeof(float) * s->ncell, cudaMemcpyHostToDevice));
+            st = cu(cudaMemcpy(ptr[k], buf.data(), bytes[k], cudaMemcpyHostToDevice));
     }
     std::fclose(f);
     if (st != FDTD_OK)
@@ -409,7 +438,7 @@ int fdtd_solver_restore(fdtd_solver *s, const char *path)
     // produced the saved H read (zero where H is never updated); copy it too
     if (s->kernel != FDTD_KERNEL_TWO_PASS)
         for (int c = 0; c < 3 && st == FDTD_OK; c++)
-            st = cu(cudaMemcpy(s->h[(h.steps + 1) & 1][c], arrs[c], sizeof(float) * s->ncell,
+            st = cu(cudaMemcpy(s->h[(h.steps + 1) & 1][c], ptr[c], sizeof(float) * s->ncell,
                                cudaMemcpyDeviceToDevice));
     int steps = h.steps;
     if (st == FDTD_OK)

@@ -55,6 +55,8 @@ struct NativeConsts {
     int fuse_mur_x;        // the single-pass kernel applies the x-face Mur updates and the Mur
                            // kernel of the same step skips them (set for both launches or neither)
     const float4 *mur_x;   // per x-face cell: 1/(dt+q_self), dt-q_nbr, dt+q_nbr, dt-q_self, [face][z][y]
+    uint32_t *r_exp;       // compact form with 16-bit R: the segment exponent words (see r16_words),
+                           // and d_cur == d_prev hold int16 values; null in the other forms
     const float *h_in[3];
     float *h_out[3];
     const float *e_cur[3];
@@ -86,9 +88,25 @@ int launch_de(const NativeConsts &c, cudaStream_t s);
 int launch_mur(const NativeConsts &c, cudaStream_t s);
 // Single-pass step: H, D, sources and E in one z-marching kernel, then Mur.
 int launch_step(const NativeConsts &c, cudaStream_t s);
+
+// Compact form with R stored in 16 bits: R_k of a cell is an int16 q times
+// 2^(b - 127), where b (1..254) is shared by the 32 cells x0 .. x0+31 of one
+// row of one plane (x0 a multiple of 32) and held in byte k of that row
+// segment's exponent word.  Words are laid out [z][x / 32][y] with each
+// segment's column padded to r16_rows(ny) words (TMA stages a tile's 8 rows
+// as one 32-byte box).  An all-zero word decodes to R = 0.
+__host__ __device__ inline int r16_segments(int nx) { return (nx + 31) / 32; }
+__host__ __device__ inline int r16_rows(int ny) { return (ny + 7) & ~7; }
+__host__ __device__ inline size_t r16_words(int nx, int ny, int nz)
+{
+    return (size_t)nz * r16_segments(nx) * r16_rows(ny);
+}
 // Compact nine-field step (d_cur == d_prev == R, updated in place) + Mur.
 int launch_step_compact(const NativeConsts &c, cudaStream_t s);
 int launch_h_e_compact(const NativeConsts &c, cudaStream_t s);
+// The same with R in 16 bits (c.r_exp set): the step, and its first kernel.
+int launch_step_compact16(const NativeConsts &c, cudaStream_t s);
+int launch_h_e_compact16(const NativeConsts &c, cudaStream_t s);
 
 // The kernels of one step in launch order, each launchable on its own (for
 // per-kernel event timing).
@@ -103,7 +121,9 @@ int step_kernels(int kernel_kind, const NativeConsts &c, StepKernel *out, int ma
 int launch_h_de_fused(const NativeConsts &c, cudaStream_t s);
 
 // Tensor maps of one single-pass launch: E^n (3), H_old (3), D^n (3),
-// D^{n-1} (3), E^{n-1} (3), material classes (1).
+// D^{n-1} (3), E^{n-1} (3), material classes (1).  Compact form: R (3)
+// after the six halo maps, then the classes; with 16-bit R the exponent
+// words follow the classes.
 struct FusedMaps {
     CUtensorMap m[16];
 };
@@ -139,18 +159,19 @@ struct BatchLaunch {
     int persistent_ctas;
     int compact;      // the batch's solves keep the compact state (d_cur == d_prev == R)
     int max_classes;  // largest class count of the batch's solves (shared-memory table)
+    int r16;          // the compact state holds R in 16 bits (compact is set too)
 };
 
 // Tensor maps of a single-pass launch over c's buffers (false: not encodable).
 bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps);
-bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps);
+bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps, bool r16 = false);
 int fused_tile_height();
 int fused_zchunk(int nz);
 int compact_zchunk(int nz);
 int zchunk_limited(int nz, int max_planes);  // nz in equal chunks of at most max_planes planes
 // One batched step: fused kernel over all units, Mur faces, step counters.
 int launch_batch_step(const BatchLaunch &b, cudaStream_t s);
-int batch_persistent_ctas(bool compact, int nclasses);
+int batch_persistent_ctas(bool compact, int nclasses, bool r16 = false);
 
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);

@@ -42,6 +42,14 @@ fdtd_native_fields step_fields(const fdtd_solver *s, int n)
     return f;
 }
 
+NativeConsts solver_consts(const fdtd_solver *s, int n)
+{
+    const fdtd_native_fields f = step_fields(s, n);
+    NativeConsts c = make_consts(s->plan, &f, n);
+    c.r_exp = s->rexp;
+    return c;
+}
+
 // Device buffer holding `field` after `count` completed steps.
 const float *field_buffer(const fdtd_solver *s, int field, int count)
 {
@@ -50,7 +58,7 @@ const float *field_buffer(const fdtd_solver *s, int field, int count)
         const int idx = s->kernel != FDTD_KERNEL_TWO_PASS ? (count & 1) : 0;
         return s->h[idx][comp];
     }
-    if (field < 6 && s->kernel == FDTD_KERNEL_COMPACT)
+    if (field < 6 && stores_no_d(s->kernel))
         return nullptr;  // D is not stored
     // E^{count}, D^{count} live in slot (count - 1) % 2; before any step both slots are zero.
     const int slot = count > 0 ? ((count - 1) & 1) : 0;
@@ -72,8 +80,7 @@ int cu(cudaError_t e) { return e == cudaSuccess ? FDTD_OK : (int)e; }
 
 int enqueue_step(fdtd_solver *s, int n)
 {
-    const fdtd_native_fields f = step_fields(s, n);
-    NativeConsts c = make_consts(s->plan, &f, n);
+    NativeConsts c = solver_consts(s, n);
     c.step_counter = s->counter;
     // in a graph the step's first kernel follows the previous step's Mur
     // kernel unless a monitor kernel runs between them
@@ -83,6 +90,8 @@ int enqueue_step(fdtd_solver *s, int n)
         st = launch_step(c, s->stream);
     } else if (s->kernel == FDTD_KERNEL_COMPACT) {
         st = launch_step_compact(c, s->stream);
+    } else if (s->kernel == FDTD_KERNEL_COMPACT_R16) {
+        st = launch_step_compact16(c, s->stream);
     } else {
         st = launch_h(c, s->stream);
         if (st == FDTD_OK)
@@ -296,7 +305,7 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     if (!cfg || !out || !cfg->params || !cfg->material || !cfg->specs)
         return FDTD_ERR_INVALID;
     if (cfg->kernel != FDTD_KERNEL_SINGLE_PASS && cfg->kernel != FDTD_KERNEL_TWO_PASS &&
-        cfg->kernel != FDTD_KERNEL_COMPACT)
+        cfg->kernel != FDTD_KERNEL_COMPACT && cfg->kernel != FDTD_KERNEL_COMPACT_R16)
         return FDTD_ERR_INVALID;
     const FdtdParams *p = cfg->params;
     int st = cu(cudaSetDevice(cfg->device));
@@ -325,11 +334,15 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         return st;
     }
     // H: two buffers for the single-pass kernels, one for the two-pass pair;
-    // E: two slots; D: two slots, or one R array for the compact form
+    // E: two slots; D: two slots, or one R array for the compact form (int16
+    // R and its exponent words for the 16-bit form)
+    const bool r16 = cfg->kernel == FDTD_KERNEL_COMPACT_R16;
     const int nh = cfg->kernel == FDTD_KERNEL_TWO_PASS ? 1 : 2;
-    const int nd = cfg->kernel == FDTD_KERNEL_COMPACT ? 1 : 2;
+    const int nd = stores_no_d(cfg->kernel) ? 1 : 2;
     const size_t fbytes = ((n * sizeof(float)) + 255) & ~size_t(255);
-    const size_t total = fbytes * (3 * nh + 6 + 3 * nd) + ((n + 255) & ~size_t(255)) + 256;
+    const size_t dbytes = r16 ? ((n * sizeof(int16_t)) + 255) & ~size_t(255) : fbytes;
+    const size_t xbytes = r16 ? ((r16_words(p->nx, p->ny, p->nz) * sizeof(uint32_t)) + 255) & ~size_t(255) : 0;
+    const size_t total = fbytes * (3 * nh + 6) + dbytes * 3 * nd + xbytes + ((n + 255) & ~size_t(255)) + 256;
     st = cu(cudaMalloc(&s->d_block, total));
     if (st == FDTD_OK) {
         char *q = s->d_block;
@@ -343,11 +356,15 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
             for (int k = 0; k < 3; k++, q += fbytes)
                 s->e[b][k] = reinterpret_cast<float *>(q);
         for (int b = 0; b < nd; b++)
-            for (int k = 0; k < 3; k++, q += fbytes)
+            for (int k = 0; k < 3; k++, q += dbytes)
                 s->d[b][k] = reinterpret_cast<float *>(q);
         if (nd == 1)
             for (int k = 0; k < 3; k++)
                 s->d[1][k] = s->d[0][k];
+        if (r16) {
+            s->rexp = reinterpret_cast<uint32_t *>(q);
+            q += xbytes;
+        }
         s->mat = reinterpret_cast<uint8_t *>(q);
         q += (n + 255) & ~size_t(255);
         s->counter = reinterpret_cast<int *>(q);
@@ -496,7 +513,7 @@ int fdtd_solver_set_snapshots(fdtd_solver *s, const fdtd_snapshot_spec *spec)
         return FDTD_ERR_INVALID;
     if (sp.format < FDTD_SNAPSHOT_TEXT || sp.format > FDTD_SNAPSHOT_TEXT_AND_BINARY)
         return FDTD_ERR_INVALID;
-    if (s->kernel == FDTD_KERNEL_COMPACT && (sp.field_mask & (7u << FDTD_FIELD_DX)))
+    if (stores_no_d(s->kernel) && (sp.field_mask & (7u << FDTD_FIELD_DX)))
         return FDTD_ERR_INVALID;  // D is not stored
     for (int f = 0; f < FDTD_FIELD_COUNT; f++)
         if (sp.field_mask & (1u << f))
@@ -532,16 +549,14 @@ int fdtd_solver_profile(fdtd_solver *s, int nsteps, float *avg_ms, int max_kerne
         s->copy_pending = false;
     }
     StepKernel ks[8];
-    const fdtd_native_fields f0 = step_fields(s, s->steps);
-    const int nk = step_kernels(s->kernel, make_consts(s->plan, &f0, s->steps), ks, 8);
+    const int nk = step_kernels(s->kernel, solver_consts(s, s->steps), ks, 8);
     std::vector<cudaEvent_t> ev((size_t)nsteps * (nk + 1), nullptr);
     for (auto &e : ev)
         if (st == FDTD_OK)
             st = cu(cudaEventCreate(&e));
     for (int k = 0; k < nsteps && st == FDTD_OK; k++) {
         const int n = s->steps;
-        const fdtd_native_fields f = step_fields(s, n);
-        NativeConsts c = make_consts(s->plan, &f, n);
+        NativeConsts c = solver_consts(s, n);
         c.step_counter = s->counter;
         c.fuse_mur_x = s->kernel != FDTD_KERNEL_TWO_PASS;  // as launch_step sets it
         cudaEvent_t *e = &ev[(size_t)k * (nk + 1)];
@@ -578,8 +593,7 @@ const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k)
     if (!s || k < 0)
         return nullptr;
     StepKernel ks[8];
-    const fdtd_native_fields f0 = step_fields(s, s->steps);
-    const int nk = step_kernels(s->kernel, make_consts(s->plan, &f0, s->steps), ks, 8);
+    const int nk = step_kernels(s->kernel, solver_consts(s, s->steps), ks, 8);
     return k < nk ? ks[k].name : nullptr;
 }
 

@@ -34,6 +34,7 @@ struct fdtd_solver {
     float *e[2][3] = {};
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
+    uint32_t *rexp = nullptr;  // FDTD_KERNEL_COMPACT_R16: exponent words (d[0] holds the int16 R)
     int *counter = nullptr;
     int steps = 0;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (parity, length) -> exec
@@ -75,6 +76,10 @@ namespace fdtd {
 
 // Pointers of step n and the device buffer of a field after `count` steps.
 fdtd_native_fields step_fields(const fdtd_solver *s, int n);
+// Kernel arguments of step n (the form's extra state included).
+NativeConsts solver_consts(const fdtd_solver *s, int n);
+// The form stores no D (the compact forms).
+inline bool stores_no_d(int kernel) { return kernel == FDTD_KERNEL_COMPACT || kernel == FDTD_KERNEL_COMPACT_R16; }
 const float *field_buffer(const fdtd_solver *s, int field, int count);
 // Monitor launch after step n (nothing when no monitor is installed).
 int launch_monitor(fdtd_solver *s, int n);

@@ -38,25 +38,32 @@ using namespace tma;
 static_assert(FTX == FUSED_TILE_X, "x-face Mur fusion assumes 32-column tiles");
 
 
-// Shared-memory layout of one stage for NT tile arrays (9: D^n, D^{n-1},
-// E^{n-1} of the D form; 3: R of the compact form).
-template <int TY, int NT = 9>
+// Shared-memory layout of one stage for NT tile arrays of TB-byte elements
+// (9 floats: D^n, D^{n-1}, E^{n-1} of the D form; 3 floats: R of the compact
+// form; 3 int16: R of the compact form with 16-bit R, which also stages its
+// TY exponent words, XB bytes).
+template <int TY, int NT = 9, int TB = 4, int XB = 0>
 struct Geo {
     static constexpr int EW = FTX + 8, EH = TY + 2;   // E^n box: x0-4 .. x0+TX+3, y0-1 .. y0+TY
     static constexpr int HW = FTX + 4, HH = TY + 1;   // H box: x0-4 .. x0+TX-1, y0-1 .. y0+TY-1
-    static constexpr int E_BYTES = EW * EH * 4, H_BYTES = HW * HH * 4, T_BYTES = FTX * TY * 4, M_BYTES = FTX * TY;
+    static constexpr int E_BYTES = EW * EH * 4, H_BYTES = HW * HH * 4, T_BYTES = FTX * TY * TB, M_BYTES = FTX * TY;
     static constexpr int OFF_E = 0;
     static constexpr int OFF_H = OFF_E + 3 * pad128(E_BYTES);
     static constexpr int OFF_T = OFF_H + 3 * pad128(H_BYTES);
-    static constexpr int OFF_M = OFF_T + NT * pad128(T_BYTES);
+    static constexpr int OFF_X = OFF_T + NT * pad128(T_BYTES);
+    static constexpr int OFF_M = OFF_X + pad128(XB);
     static constexpr int STAGE = pad128(OFF_M + M_BYTES);
     static constexpr int HNW = FTX + 1, HNH = TY + 1;  // H^{n+1/2} plane incl. low halo
     static constexpr int HN_BYTES = pad128(3 * HNW * HNH * 4);
     // expected transaction bytes per plane kind
-    static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + unsigned(NT) * T_BYTES + M_BYTES;
+    static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + unsigned(NT) * T_BYTES + XB + M_BYTES;
     static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
     static constexpr unsigned TX_EPI = 3u * E_BYTES;
 };
+
+// Stage geometry of a form.
+template <int TY, bool COMPACT, bool R16>
+using GeoOf = Geo<TY, COMPACT ? 3 : 9, R16 ? 2 : 4, R16 ? TY * 4 : 0>;
 
 struct FusedArgs {
     NativeConsts c;
@@ -65,12 +72,13 @@ struct FusedArgs {
 
 // TMA: one thread arms the stage's barrier and issues the plane's boxes.
 // With arm_only (the stall test hook) the barrier expects the plane's bytes
-// but no copy is issued.
-template <int TY, int NT = 9>
+// but no copy is issued.  The tile maps follow the six halo maps, then the
+// classes, then (16-bit R) the exponent words.
+template <int TY, int NT = 9, int TB = 4, int XB = 0>
 __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
                                 int z, bool arm_only = false)
 {
-    using G = Geo<TY, NT>;
+    using G = Geo<TY, NT, TB, XB>;
     const unsigned bytes = kind == PLANE_FULL ? G::TX_FULL : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI);
     mbar_expect_tx(bar, bytes);
     if (arm_only)
@@ -86,15 +94,18 @@ __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uin
     for (int k = 0; k < NT; k++)
         tma_load_3d(smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), &maps.m[6 + k], x0, y0, z, bar);
     tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[6 + NT], x0, y0, z, bar);
+    if (XB > 0)  // exponent words of rows y0 .. y0+TY-1 of segment x0 / 32 (y0 * 4 bytes: 16-byte aligned)
+        tma_load_3d(smem_addr(stage + G::OFF_X), &maps.m[7 + NT], y0, x0 / FTX, z, bar);
 }
 
 // Generic: every thread copies part of each box with 4-byte cp.async
-// (zero-filled outside the grid); the material classes are read separately.
-template <int TY, int NT = 9>
+// (zero-filled outside the grid); the material classes are read separately,
+// and so are 16-bit R and its exponent words (no tiles staged for them).
+template <int TY, int NT = 9, int TB = 4, int XB = 0>
 __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage, int kind, int x0, int y0, int z,
                                     int tid)
 {
-    using G = Geo<TY, NT>;
+    using G = Geo<TY, NT, TB, XB>;
     constexpr int NTH = FTX * TY;
     const int nx = c.nx, ny = c.ny, pitch = c.pitch;
     const size_t plane = (size_t)pitch * ny;
@@ -116,8 +127,9 @@ __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage,
         return;
     const float *tiles[9] = {c.d_cur[0], c.d_cur[1], c.d_cur[2], c.d_prev[0], c.d_prev[1],
                              c.d_prev[2], c.e_prev[0], c.e_prev[1], c.e_prev[2]};
-    for (int k = 0; k < NT; k++)
-        box(tiles[k], smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), x0, y0, FTX, TY);
+    if (TB == 4)
+        for (int k = 0; k < NT; k++)
+            box(tiles[k], smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), x0, y0, FTX, TY);
 }
 
 // ---------------------------------------------------------------- the kernel
@@ -134,18 +146,50 @@ __device__ __forceinline__ bool unit_has_source(const NativeConsts &c, int x0, i
     return any;
 }
 
+// ---- 16-bit R (layout: r16_segments / r16_rows / r16_words)
+
+// Index of the exponent word of row y, segment bx, plane z.
+__device__ __forceinline__ size_t r16_word(const NativeConsts &c, int z, int bx, int y)
+{
+    return ((size_t)z * r16_segments(c.nx) + bx) * r16_rows(c.ny) + y;
+}
+
+// R_k of a cell from its int16 value q and its segment's word w (exact:
+// q has at most 16 significant bits and 2^(b-127) is a normal float; w = 0
+// gives 0).
+__device__ __forceinline__ float r16_decode(int q, uint32_t w, int k)
+{
+    return __int2float_rn(q) * __uint_as_float(((w >> (8 * k)) & 0xffu) << 23);
+}
+
+// Warp-collective (every lane of the warp calls it; one warp is one row
+// segment): b = e - 14, at least 1, for the largest |r| of the segment with
+// biased exponent e, and this lane's q = round-to-nearest-even(r 2^(127-b))
+// saturated to int16.  The largest value keeps 15 significant bits; the
+// scaling by a power of two is exact.  Lanes outside the grid pass r = 0.
+__device__ __forceinline__ int r16_encode(float r, uint32_t &b)
+{
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(r) & 0x7fffffffu);
+    b = (unsigned)max((int)(m >> 23) - 14, 1);
+    const float v = r * __uint_as_float((254u - b) << 23);
+    short q;
+    asm("cvt.rni.sat.s16.f32 %0, %1;" : "=h"(q) : "f"(v));
+    return q;
+}
+
 // One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
 // stage ring and its barriers continue from earlier units of the same CTA:
 // g0 counts the planes this CTA has staged before.  Returns false when a
 // bounded wait gave up (the error flag is set; the CTA must stop).  stall
 // (read by thread 0 only): leave the second plane's copies unissued.
-template <int TY, int S, bool TMA, bool COMPACT = false>
+template <int TY, int S, bool TMA, bool COMPACT = false, bool R16 = false>
 __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMaps &maps, int zchunk, int bx, int by,
                                            int bz, unsigned char *smem, const DebyeCoef *coef, uint64_t *bars,
                                            unsigned g0, bool stall = false)
 {
-    constexpr int NT = COMPACT ? 3 : 9;
-    using G = Geo<TY, NT>;
+    static_assert(COMPACT || !R16, "16-bit R is a compact-form layout");
+    constexpr int NT = COMPACT ? 3 : 9, TB = R16 ? 2 : 4, XB = R16 ? TY * 4 : 0;
+    using G = Geo<TY, NT, TB, XB>;
     const int nx = c.nx, ny = c.ny, nz = c.nz;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FTX + tx;
     const int x0 = bx * FTX, y0 = by * TY;
@@ -165,10 +209,10 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             const int z = p0 + k;
             if (TMA) {
                 if (tid == 0)
-                    issue_plane_tma<TY, NT>(maps, stage(k), bar(k), plane_kind(z, zc0, zc1), x0, y0, z,
+                    issue_plane_tma<TY, NT, TB, XB>(maps, stage(k), bar(k), plane_kind(z, zc0, zc1), x0, y0, z,
                                             stall && k == 1);
             } else {
-                issue_plane_generic<TY, NT>(c, stage(k), plane_kind(z, zc0, zc1), x0, y0, z, tid);
+                issue_plane_generic<TY, NT, TB, XB>(c, stage(k), plane_kind(z, zc0, zc1), x0, y0, z, tid);
             }
         }
         if (!TMA)
@@ -328,11 +372,36 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
 
             float ey_new = 0.0f, ez_new = 0.0f;  // this lane's E^{n+1} y, z (for the x-face lanes)
             if constexpr (COMPACT) {
+            const size_t i = (size_t)z * plane + col;
+            float rn0 = 0.0f, rn1 = 0.0f, rn2 = 0.0f;  // R^{n+1} (16-bit R: 0 where not updated)
             if (in_dom) {
-                const size_t i = (size_t)z * plane + col;
-                const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
                 const int t = ty * FTX + tx;
-                const float r0 = T[0 * TS + t], r1 = T[1 * TS + t], r2 = T[2 * TS + t];
+                float r0, r1, r2;
+                if constexpr (R16) {
+                    int q0, q1, q2;
+                    uint32_t w;
+                    if (TMA) {
+                        const int16_t *T = reinterpret_cast<const int16_t *>(stage(k) + G::OFF_T);
+                        constexpr int TS16 = pad128(G::T_BYTES) / 2;
+                        q0 = T[t];
+                        q1 = T[TS16 + t];
+                        q2 = T[2 * TS16 + t];
+                        w = reinterpret_cast<const uint32_t *>(stage(k) + G::OFF_X)[ty];
+                    } else {
+                        q0 = reinterpret_cast<const int16_t *>(c.d_cur[0])[i];
+                        q1 = reinterpret_cast<const int16_t *>(c.d_cur[1])[i];
+                        q2 = reinterpret_cast<const int16_t *>(c.d_cur[2])[i];
+                        w = c.r_exp[r16_word(c, z, bx, y)];
+                    }
+                    r0 = r16_decode(q0, w, 0);
+                    r1 = r16_decode(q1, w, 1);
+                    r2 = r16_decode(q2, w, 2);
+                } else {
+                    const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
+                    r0 = T[0 * TS + t];
+                    r1 = T[1 * TS + t];
+                    r2 = T[2 * TS + t];
+                }
                 uint8_t cls;
                 if (TMA) {
                     cls = (stage(k) + G::OFF_M)[t];
@@ -381,17 +450,39 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     if (ex_on) {
                         const float e = ea(0, r, cc);
                         c.e_prev[0][i] = kc.c * (kc.d * e + k12 * g0 + r0);
-                        c.d_prev[0][i] = -kc.a * e - kc.two_tau * g0;
+                        rn0 = -kc.a * e - kc.two_tau * g0;
+                        if constexpr (!R16)
+                            c.d_prev[0][i] = rn0;
                     }
                     if (eyz_on) {
                         const float e1 = ea(1, r, cc), e2 = ea(2, r, cc);
                         ey_new = kc.c * (kc.d * e1 + k12 * g1 + r1);
                         ez_new = kc.c * (kc.d * e2 + k12 * g2 + r2);
                         c.e_prev[1][i] = ey_new;
-                        c.d_prev[1][i] = -kc.a * e1 - kc.two_tau * g1;
+                        rn1 = -kc.a * e1 - kc.two_tau * g1;
                         c.e_prev[2][i] = ez_new;
-                        c.d_prev[2][i] = -kc.a * e2 - kc.two_tau * g2;
+                        rn2 = -kc.a * e2 - kc.two_tau * g2;
+                        if constexpr (!R16) {
+                            c.d_prev[1][i] = rn1;
+                            c.d_prev[2][i] = rn2;
+                        }
                     }
+                }
+            }
+            if constexpr (R16) {
+                // every cell of the row segment is rewritten with the
+                // segment's new exponent (cells whose E is never updated
+                // keep R = 0, as in the 32-bit compact form)
+                if (y < ny) {  // uniform over the warp: one warp is one row
+                    uint32_t b0, b1, b2;
+                    const int q0 = r16_encode(rn0, b0), q1 = r16_encode(rn1, b1), q2 = r16_encode(rn2, b2);
+                    if (x < nx) {
+                        reinterpret_cast<int16_t *>(c.d_prev[0])[i] = (int16_t)q0;
+                        reinterpret_cast<int16_t *>(c.d_prev[1])[i] = (int16_t)q1;
+                        reinterpret_cast<int16_t *>(c.d_prev[2])[i] = (int16_t)q2;
+                    }
+                    if (tx == 0)
+                        c.r_exp[r16_word(c, z, bx, y)] = b0 | (b1 << 8) | (b2 << 16);
                 }
             }
             } else {
@@ -496,12 +587,12 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             if (tid == 0 && kn < nplanes) {
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const int zn = p0 + kn;
-                issue_plane_tma<TY, NT>(maps, stage(kn), bar(kn), plane_kind(zn, zc0, zc1), x0, y0, zn);
+                issue_plane_tma<TY, NT, TB, XB>(maps, stage(kn), bar(kn), plane_kind(zn, zc0, zc1), x0, y0, zn);
             }
         } else {
             if (kn < nplanes) {
                 const int zn = p0 + kn;
-                issue_plane_generic<TY, NT>(c, stage(kn), plane_kind(zn, zc0, zc1), x0, y0, zn, tid);
+                issue_plane_generic<TY, NT, TB, XB>(c, stage(kn), plane_kind(zn, zc0, zc1), x0, y0, zn, tid);
             }
             cp_async_commit();
         }
@@ -517,16 +608,15 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
 template <int S>
 __host__ __device__ constexpr int bars_bytes() { return (S * 8 + 15) & ~15; }
 
-template <int TY, int S, int NT = 9>
+template <int S, class G>
 __host__ __device__ constexpr int fused_smem_bytes(int nclasses)
 {
-    return 128 + S * Geo<TY, NT>::STAGE + Geo<TY, NT>::HN_BYTES + bars_bytes<S>() + nclasses * (int)sizeof(DebyeCoef);
+    return 128 + S * G::STAGE + G::HN_BYTES + bars_bytes<S>() + nclasses * (int)sizeof(DebyeCoef);
 }
 
-template <int TY, int S, bool TMA, int NT = 9>
+template <int S, bool TMA, class G>
 __device__ __forceinline__ void fused_cta_setup(unsigned char *smem, DebyeCoef **coef, uint64_t **bars)
 {
-    using G = Geo<TY, NT>;
     *bars = reinterpret_cast<uint64_t *>(smem + S * G::STAGE + G::HN_BYTES);
     *coef = reinterpret_cast<DebyeCoef *>(smem + S * G::STAGE + G::HN_BYTES + bars_bytes<S>());
     const int tid = threadIdx.y * FTX + threadIdx.x;
@@ -547,7 +637,7 @@ __device__ __forceinline__ void load_coef(const NativeConsts &c, DebyeCoef *coef
 }
 
 // One solve: CTA (bx, by, bz) processes one unit.
-template <int TY, int S, bool TMA, bool COMPACT>
+template <int TY, int S, bool TMA, bool COMPACT, bool R16 = false>
 __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_constant__ FusedArgs a,
                                                              const __grid_constant__ FusedMaps maps)
 {
@@ -555,7 +645,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     unsigned char *smem = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
     DebyeCoef *coef;
     uint64_t *bars;
-    fused_cta_setup<TY, S, TMA, COMPACT ? 3 : 9>(smem, &coef, &bars);
+    fused_cta_setup<S, TMA, GeoOf<TY, COMPACT, R16>>(smem, &coef, &bars);
     load_coef(a.c, coef, FTX * TY);
     const int bz = blockIdx.z;
     if (a.c.overlap_prev) {
@@ -578,7 +668,8 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
     if (TMA && a.c.stall_once && blockIdx.x == 0 && blockIdx.y == 0 && bz == 0 && threadIdx.x == 0 &&
         threadIdx.y == 0)
         stall = atomicExch(a.c.stall_once, 0) != 0;
-    fused_unit<TY, S, TMA, COMPACT>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, smem, coef, bars, 0u, stall);
+    fused_unit<TY, S, TMA, COMPACT, R16>(a.c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, smem, coef, bars, 0u,
+                                         stall);
 }
 
 // Many solves: persistent CTAs take work units from a counter; a unit's solve
@@ -587,7 +678,7 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
 // The compact form is bounded for 4 resident CTAs per SM (the 64-solve
 // workload ran 4.8 % faster than with 5: fewer units in flight, more
 // registers per thread).
-template <int TY, int S, bool COMPACT>
+template <int TY, int S, bool COMPACT, bool R16 = false>
 __global__ void __launch_bounds__(FTX *TY, COMPACT ? 4 : 3) batch_step_kernel(const BatchDesc *__restrict__ descs, int nsolves,
                                                              int total_units, int *work_counter)
 {
@@ -597,7 +688,7 @@ __global__ void __launch_bounds__(FTX *TY, COMPACT ? 4 : 3) batch_step_kernel(co
     __shared__ int s_unit, s_solve;
     DebyeCoef *coef;
     uint64_t *bars;
-    fused_cta_setup<TY, S, true, COMPACT ? 3 : 9>(smem, &coef, &bars);
+    fused_cta_setup<S, true, GeoOf<TY, COMPACT, R16>>(smem, &coef, &bars);
     const int tid = threadIdx.y * FTX + threadIdx.x;
     int loaded = -1;
     unsigned g = 0;
@@ -642,7 +733,7 @@ __global__ void __launch_bounds__(FTX *TY, COMPACT ? 4 : 3) batch_step_kernel(co
             const int by = rem / d.tiles_x, bx = rem % d.tiles_x;
             const int zc0 = bz * d.zchunk, zc1 = min(s_c.nz, zc0 + d.zchunk);
             const int nplanes = min(zc1, s_c.nz - 1) - max(zc0 - 1, 0) + 1;
-            if (!fused_unit<TY, S, true, COMPACT>(s_c, d.maps[par], d.zchunk, bx, by, bz, smem, coef, bars, g))
+            if (!fused_unit<TY, S, true, COMPACT, R16>(s_c, d.maps[par], d.zchunk, bx, by, bz, smem, coef, bars, g))
                 return;
             g += (unsigned)nplanes;
         }
@@ -699,19 +790,19 @@ constexpr int TY_SEL = FDTD_TILE_ROWS;
 constexpr int S_SEL = FDTD_RING_STAGES;
 
 
-template <bool TMA, bool COMPACT>
+template <bool TMA, bool COMPACT, bool R16 = false>
 int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
-    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA, COMPACT>;
-    constexpr int NT = COMPACT ? 3 : 9;
+    auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA, COMPACT, R16>;
+    using G = GeoOf<TY_SEL, COMPACT, R16>;
     static std::once_flag once;
     std::call_once(once, [&] {
         cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             fused_smem_bytes<TY_SEL, S_SEL, NT>(FDTD_MAX_CLASSES));
+                             fused_smem_bytes<S_SEL, G>(FDTD_MAX_CLASSES));
     });
     if (a.c.nclasses < 1 || a.c.nclasses > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
-    const int smem = fused_smem_bytes<TY_SEL, S_SEL, NT>(a.c.nclasses);
+    const int smem = fused_smem_bytes<S_SEL, G>(a.c.nclasses);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
     cfg.blockDim = dim3(FTX, TY_SEL);
@@ -763,11 +854,12 @@ bool fused_uses_tma(const NativeConsts &c)
 
 // Tensor maps of one step: E^n and H^{n-1/2} halo boxes (0-5), the tile
 // arrays (D form: D^n, D^{n-1}, E^{n-1} at 6-14; compact form: R at 6-8) and
-// the class volume after them.
-bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps)
+// the class volume after them; with 16-bit R (int16 tiles at 6-8) the
+// exponent words at 10 (box: one segment's TY rows).
+bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps, bool r16)
 {
     memset(maps, 0, sizeof *maps);
-    if (!fused_uses_tma(c))
+    if (!fused_uses_tma(c) || (r16 && (!compact || !c.r_exp || !aligned16(c.r_exp))))
         return false;
     auto fn = encode_fn();
     using G = Geo<TY_SEL>;
@@ -777,10 +869,22 @@ bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps)
     for (int k = 0; k < 3 && ok; k++) {
         ok &= encode_map(fn, &maps->m[k], c.e_cur[k], false, c.nx, c.ny, c.nz, c.pitch, G::EW, G::EH);
         ok &= encode_map(fn, &maps->m[3 + k], c.h_in[k], false, c.nx, c.ny, c.nz, c.pitch, G::HW, G::HH);
-        for (int t = 0; t < ntile_sets; t++)
-            ok &= encode_map(fn, &maps->m[6 + 3 * t + k], tiles[t][k], false, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+        for (int t = 0; t < ntile_sets; t++) {
+            if (r16)  // pitch % 16 == 0: rows of 2-byte values keep 16-byte strides
+                ok &= encode_map_3d(fn, &maps->m[6 + k], tiles[t][k], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, c.nx, c.ny,
+                                    c.nz, (size_t)c.pitch, (size_t)c.pitch * c.ny, FTX, TY_SEL);
+            else
+                ok &= encode_map(fn, &maps->m[6 + 3 * t + k], tiles[t][k], false, c.nx, c.ny, c.nz, c.pitch, FTX,
+                                 TY_SEL);
+        }
     }
-    return ok && encode_map(fn, &maps->m[6 + 3 * ntile_sets], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+    ok = ok && encode_map(fn, &maps->m[6 + 3 * ntile_sets], c.mat, true, c.nx, c.ny, c.nz, c.pitch, FTX, TY_SEL);
+    if (ok && r16) {
+        const int rows = r16_rows(c.ny), segs = r16_segments(c.nx);
+        ok = encode_map_3d(fn, &maps->m[10], c.r_exp, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, rows, segs, c.nz,
+                           (size_t)rows, (size_t)rows * segs, TY_SEL, 1);
+    }
+    return ok;
 }
 
 bool encode_fused_maps(const NativeConsts &c, FusedMaps *maps) { return encode_step_maps(c, false, maps); }
@@ -789,26 +893,29 @@ int fused_tile_height() { return TY_SEL; }
 
 // Shared memory of the persistent batch kernel: tiles of the form and a class
 // table for the batch's largest class count.
-template <bool COMPACT>
-int batch_smem(int nclasses) { return fused_smem_bytes<TY_SEL, S_SEL, COMPACT ? 3 : 9>(nclasses); }
+template <bool COMPACT, bool R16 = false>
+int batch_smem(int nclasses) { return fused_smem_bytes<S_SEL, GeoOf<TY_SEL, COMPACT, R16>>(nclasses); }
 
-template <bool COMPACT>
+template <bool COMPACT, bool R16 = false>
 int batch_ctas_impl(int nclasses)
 {
-    auto kernel = batch_step_kernel<TY_SEL, S_SEL, COMPACT>;
+    auto kernel = batch_step_kernel<TY_SEL, S_SEL, COMPACT, R16>;
     static std::once_flag once;
     std::call_once(once, [&] {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, batch_smem<COMPACT>(FDTD_MAX_CLASSES));
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             batch_smem<COMPACT, R16>(FDTD_MAX_CLASSES));
     });
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FTX * TY_SEL, batch_smem<COMPACT>(nclasses));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, FTX * TY_SEL, batch_smem<COMPACT, R16>(nclasses));
     return sms * (per_sm > 0 ? per_sm : 1);
 }
 
-int batch_persistent_ctas(bool compact, int nclasses)
+int batch_persistent_ctas(bool compact, int nclasses, bool r16)
 {
+    if (r16)
+        return batch_ctas_impl<true, true>(nclasses);
     return compact ? batch_ctas_impl<true>(nclasses) : batch_ctas_impl<false>(nclasses);
 }
 
@@ -816,7 +923,11 @@ int launch_batch_step(const BatchLaunch &b, cudaStream_t s)
 {
     if (b.max_classes < 1 || b.max_classes > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
-    if (b.compact)
+    if (b.r16)
+        batch_step_kernel<TY_SEL, S_SEL, true, true>
+            <<<b.persistent_ctas, dim3(FTX, TY_SEL), batch_smem<true, true>(b.max_classes), s>>>(
+                b.descs, b.nsolves, b.total_units, b.work_counter);
+    else if (b.compact)
         batch_step_kernel<TY_SEL, S_SEL, true>
             <<<b.persistent_ctas, dim3(FTX, TY_SEL), batch_smem<true>(b.max_classes), s>>>(
                 b.descs, b.nsolves, b.total_units, b.work_counter);
@@ -861,6 +972,19 @@ int launch_h_e_compact(const NativeConsts &c, cudaStream_t s)
     return launch_fused_impl<false, true>(a, maps, s);
 }
 
+int launch_h_e_compact16(const NativeConsts &c, cudaStream_t s)
+{
+    if (c.d_cur[0] != c.d_prev[0] || c.d_cur[1] != c.d_prev[1] || c.d_cur[2] != c.d_prev[2] || !c.r_exp)
+        return FDTD_ERR_INVALID;  // R and its exponent words are updated in place
+    FusedArgs a;
+    a.c = c;
+    a.zchunk = compact_zchunk(c.nz);
+    FusedMaps maps;
+    if (encode_step_maps(c, true, &maps, true))
+        return launch_fused_impl<true, true, true>(a, maps, s);
+    return launch_fused_impl<false, true, true>(a, maps, s);
+}
+
 int launch_step(const NativeConsts &c0, cudaStream_t s)
 {
     NativeConsts c = c0;
@@ -881,14 +1005,26 @@ int launch_step_compact(const NativeConsts &c0, cudaStream_t s)
     return st;
 }
 
+int launch_step_compact16(const NativeConsts &c0, cudaStream_t s)
+{
+    NativeConsts c = c0;
+    c.fuse_mur_x = 1;
+    int st = launch_h_e_compact16(c, s);
+    if (st == FDTD_OK)
+        st = launch_mur(c, s);
+    return st;
+}
+
 int step_kernels(int kernel_kind, const NativeConsts &, StepKernel *out, int max)
 {
     static const StepKernel single[] = {{"fused_step", launch_h_de_fused}, {"mur", launch_mur}};
     static const StepKernel compact[] = {{"compact_step", launch_h_e_compact}, {"mur", launch_mur}};
+    static const StepKernel compact16[] = {{"compact16_step", launch_h_e_compact16}, {"mur", launch_mur}};
     static const StepKernel two[] = {{"h", launch_h}, {"de", launch_de}, {"mur", launch_mur}};
     const StepKernel *src = kernel_kind == FDTD_KERNEL_SINGLE_PASS ? single
-                            : kernel_kind == FDTD_KERNEL_COMPACT ? compact
-                                                                   : two;
+                            : kernel_kind == FDTD_KERNEL_COMPACT   ? compact
+                            : kernel_kind == FDTD_KERNEL_COMPACT_R16 ? compact16
+                                                                     : two;
     const int n = kernel_kind == FDTD_KERNEL_TWO_PASS ? 3 : 2;
     for (int k = 0; k < n && k < max; k++)
         out[k] = src[k];

@@ -117,19 +117,27 @@ inline PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
+// Tensor map of a 3-D array of es-byte elements of type dt: dims (d0, d1,
+// d2), element strides s1 between rows and s2 between planes, box (b0, b1, 1).
+inline bool encode_map_3d(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void *base,
+                          CUtensorMapDataType dt, size_t es, int d0, int d1, int d2, size_t s1, size_t s2, int b0,
+                          int b1)
+{
+    cuuint64_t dims[3] = {(cuuint64_t)d0, (cuuint64_t)d1, (cuuint64_t)d2};
+    cuuint64_t strides[2] = {(cuuint64_t)(s1 * es), (cuuint64_t)(s2 * es)};
+    cuuint32_t box[3] = {(cuuint32_t)b0, (cuuint32_t)b1, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = fn(m, dt, 3, const_cast<void *>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 inline bool encode_map(PFN_cuTensorMapEncodeTiled_v12000 fn, CUtensorMap *m, const void *base, bool is_u8, int nx, int ny,
                 int nz, int pitch, int bx, int by)
 {
-    const size_t es = is_u8 ? 1 : 4;
-    cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-    cuuint64_t strides[2] = {(cuuint64_t)(pitch * es), (cuuint64_t)((size_t)pitch * ny * es)};
-    cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
-    cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r =
-        fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void *>(base),
-           dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
+    return encode_map_3d(fn, m, base, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                         is_u8 ? 1 : 4, nx, ny, nz, (size_t)pitch, (size_t)pitch * ny, bx, by);
 }
 
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }

@@ -295,7 +295,16 @@ enum {
      * the same update as updateEField (fdtd_calculations.cu:141-183)
      * rearranged, 73 instead of 97 bytes of traffic per cell update.  D is not
      * stored: the D fields cannot be read, snapshotted or probed. */
-    FDTD_KERNEL_COMPACT = 2
+    FDTD_KERNEL_COMPACT = 2,
+    /* The compact form with R stored in 16 bits (no reference counterpart;
+     * the reduced-storage form): each R value is an int16 times a power of
+     * two shared by the 32 cells of one x-row segment of one plane (one
+     * exponent byte per component, the largest value of the segment keeps
+     * 15 significant bits).  H and E stay FP32 and all arithmetic is FP32;
+     * the step equals FDTD_KERNEL_COMPACT's with R rounded to that format
+     * after every step.  61.25 instead of 73 bytes of traffic per cell
+     * update.  D is not stored, as in FDTD_KERNEL_COMPACT. */
+    FDTD_KERNEL_COMPACT_R16 = 3
 };
 
 /* Field selectors; bit (1 << FDTD_FIELD_x) in snapshot masks. */
@@ -432,7 +441,8 @@ typedef struct fdtd_batch fdtd_batch;
 /* A batch of the D form (FDTD_KERNEL_SINGLE_PASS state: every field readable). */
 int fdtd_batch_create(int device, fdtd_batch **out);
 /* A batch whose solves all keep the state of `kernel`: FDTD_KERNEL_SINGLE_PASS
- * (D form) or FDTD_KERNEL_COMPACT (nine fields, D not readable). */
+ * (D form), FDTD_KERNEL_COMPACT (nine fields, D not readable) or
+ * FDTD_KERNEL_COMPACT_R16 (the same with R in 16 bits). */
 int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out);
 int fdtd_batch_destroy(fdtd_batch *b);
 /* Device bytes one D-form solve of this grid needs (state + plan), for admission. */

@@ -110,7 +110,34 @@ def test_compact_batch_matches_lone_compact_solves_and_oracle(cuda):
     b.close()
 
 
-@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT])
+def test_compact16_batch_matches_lone_solves_and_oracle(cuda):
+    """A batch of the 16-bit-R compact form: every solve equals the same form
+    run alone bit for bit (the batch pads rows to 16 cells and stages R by
+    TMA; alone, rows that are not a multiple of 16 read R directly) and the
+    oracle within the reduced-storage tolerance; it needs less memory than the
+    32-bit compact form."""
+    b = fg.Batch(kernel=fg.KERNEL_COMPACT_R16)
+    b32 = fg.Batch(kernel=fg.KERNEL_COMPACT)
+    assert b.need_bytes(64, 64, 64) < b32.need_bytes(64, 64, 64)
+    b32.close()
+    cases = [_case(k) for k in range(len(CASES))]
+    ids = [b.add(Params(c[8]), c[3], c[4], c[1], scheme=c[2]) for c in cases]
+    b.run(max(c[1] for c in cases) + 3)
+    for sid, case in zip(ids, cases):
+        dims, steps, scheme, codes, specs, sources, consts, jz, raw = case
+        assert b.steps(sid) == steps
+        got = b.fields(sid)
+        assert sorted(got) == ["ex", "ey", "ez", "hx", "hy", "hz"]
+        with fg.Solver(Params(raw), codes, specs, scheme=scheme, kernel=fg.KERNEL_COMPACT_R16) as s:
+            s.run(steps)
+            alone = s.fields()
+        for name in got:
+            assert np.array_equal(got[name].view(np.uint32), alone[name].view(np.uint32)), (dims, name)
+        assert_fields_close(got, _oracle(*case), tol=1e-3, names=list(got))
+    b.close()
+
+
+@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT, fg.KERNEL_COMPACT_R16])
 def test_autotuned_batch_gives_the_same_bits(cuda, kernel):
     """fdtd_batch_autotune times real steps of the solves at each candidate
     z-chunk limit and keeps the fastest.  A cell's update does not depend on
@@ -121,7 +148,7 @@ def test_autotuned_batch_gives_the_same_bits(cuda, kernel):
     cases = [_case(k) for k in range(len(CASES))]
     ids = [b.add(Params(c[8]), c[3], c[4], steps, scheme=c[2]) for c in cases]
     chosen = b.autotune(steps_per_trial=8)
-    cands = (8, 12, 16, 24, 32, 48, 64) if kernel == fg.KERNEL_COMPACT else (16, 24, 32, 48, 64)
+    cands = (8, 12, 16, 24, 32, 48, 64) if kernel in fg.COMPACT_KERNELS else (16, 24, 32, 48, 64)
     assert chosen in cands
     done = b.steps(ids[0])
     assert 16 * len(cands) - 8 <= done <= 16 * len(cands), done
