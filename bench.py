@@ -277,7 +277,7 @@ def precision_check(p, codes, specs, dev: int, steps: int) -> dict:
 
     nz = codes.shape[0]
     probes = precision_probes(codes)
-    freq = float(p.wave_frequency) * float(p.pulse_modulation_frequency)
+    freq = float(p.waveFrequency) * float(p.pulseModulationFrequency)
     z0, nplanes = max(0, nz // 2 - 16), min(32, nz)
 
     def run(kernel):
