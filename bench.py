@@ -55,8 +55,9 @@ FORM_BYTES = {"single": B_ALG, "two_pass": B_ALG, "compact": 73, "compact16": 61
 STATE_BYTES = {"single": 73, "two_pass": 61, "compact": 61, "compact16": 55.125}
 FORM_STATE = {
     "compact": "H (2 buffers), E (2 slots), R = -a E^{n-1} - 2 tau (D^n - D^{n-1}); D not stored",
-    "compact16": "as compact, R stored as int16 with one exponent byte per component per 32-cell row segment "
-                 "(15 significant bits for the segment's largest value); FP32 arithmetic; D not stored",
+    "compact16": "as compact, R stored as the residual R + a E^{n+1} in int16 with one exponent byte per "
+                 "component per 32-cell row segment (15 significant bits for the segment's largest value); "
+                 "source cells' R in FP32; FP32 arithmetic; D not stored",
 }
 PRECISION_PROBES = 16
 PRECISION_SEED = 2024

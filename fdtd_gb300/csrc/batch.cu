@@ -38,6 +38,7 @@ struct BatchSolve {
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
     uint32_t *rexp = nullptr;  // 16-bit R form: exponent words
+    float *rsrc = nullptr;     // ... and the source cells' FP32 R
     int *counter = nullptr;
 };
 
@@ -50,7 +51,7 @@ size_t state_bytes(int nx, int ny, int nz, bool compact, bool r16 = false)
 {
     const size_t ncell = padded_pitch(nx) * ny * nz;
     const size_t f = (ncell * sizeof(float) + 255) & ~size_t(255);
-    const size_t d = r16 ? 3 * r16_array_bytes(ncell) + r16_exp_bytes(nx, ny, nz) : (compact ? 3 : 6) * f;
+    const size_t d = r16 ? 3 * r16_array_bytes(ncell) + r16_exp_bytes(nx, ny, nz) + 256 : (compact ? 3 : 6) * f;
     return 12 * f + d + ((ncell + 255) & ~size_t(255)) + 256;
 }
 
@@ -117,6 +118,7 @@ NativeConsts solve_consts(const BatchSolve *v, int parity)
     c.pitch = v->pitch;
     c.step_counter = v->counter;
     c.r_exp = v->rexp;
+    c.r_src = v->rsrc;
     return c;
 }
 
@@ -355,6 +357,8 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         if (b->r16) {
             v->rexp = reinterpret_cast<uint32_t *>(q);
             q += r16_exp_bytes(p->nx, p->ny, p->nz);
+            v->rsrc = reinterpret_cast<float *>(q);
+            q += 256;  // R16_SRC_FLOATS floats
         }
         v->mat = reinterpret_cast<uint8_t *>(q);
         q += (v->ncell + 255) & ~size_t(255);

@@ -321,7 +321,8 @@ static const char CKP_MAGIC[8] = {'F', 'D', 'T', 'D', 'G', 'B', '3', 'C'};
 
 // Checkpoint versions: 1 holds the D form's 15 arrays (either D-form
 // kernel restores it), 2 the compact form's 12, 3 the 16-bit-R form's 9
-// float arrays, its three int16 R arrays and its exponent words.
+// float arrays, its three int16 residual arrays, its exponent words and the
+// source cells' FP32 R.
 static uint32_t ckp_version(const fdtd_solver *s)
 {
     return s->kernel == FDTD_KERNEL_COMPACT_R16 ? 3u : s->kernel == FDTD_KERNEL_COMPACT ? 2u : 1u;
@@ -350,6 +351,8 @@ static int state_blocks(fdtd_solver *s, int count, void *ptr[16], size_t bytes[1
         }
         ptr[n] = s->rexp;
         bytes[n++] = sizeof(uint32_t) * r16_words(s->nx, s->ny, s->nz);
+        ptr[n] = s->rsrc;
+        bytes[n++] = sizeof(float) * R16_SRC_FLOATS;
         return n;
     }
     for (int c = 0; c < 3; c++, n++) {

@@ -47,6 +47,7 @@ NativeConsts solver_consts(const fdtd_solver *s, int n)
     const fdtd_native_fields f = step_fields(s, n);
     NativeConsts c = make_consts(s->plan, &f, n);
     c.r_exp = s->rexp;
+    c.r_src = s->rsrc;
     return c;
 }
 
@@ -342,7 +343,9 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     const size_t fbytes = ((n * sizeof(float)) + 255) & ~size_t(255);
     const size_t dbytes = r16 ? ((n * sizeof(int16_t)) + 255) & ~size_t(255) : fbytes;
     const size_t xbytes = r16 ? ((r16_words(p->nx, p->ny, p->nz) * sizeof(uint32_t)) + 255) & ~size_t(255) : 0;
-    const size_t total = fbytes * (3 * nh + 6) + dbytes * 3 * nd + xbytes + ((n + 255) & ~size_t(255)) + 256;
+    const size_t sbytes = r16 ? 256 : 0;  // R16_SRC_FLOATS floats
+    static_assert(R16_SRC_FLOATS * sizeof(float) <= 256, "source R slots fit 256 bytes");
+    const size_t total = fbytes * (3 * nh + 6) + dbytes * 3 * nd + xbytes + sbytes + ((n + 255) & ~size_t(255)) + 256;
     st = cu(cudaMalloc(&s->d_block, total));
     if (st == FDTD_OK) {
         char *q = s->d_block;
@@ -364,6 +367,8 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         if (r16) {
             s->rexp = reinterpret_cast<uint32_t *>(q);
             q += xbytes;
+            s->rsrc = reinterpret_cast<float *>(q);
+            q += sbytes;
         }
         s->mat = reinterpret_cast<uint8_t *>(q);
         q += (n + 255) & ~size_t(255);

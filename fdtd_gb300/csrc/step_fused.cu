@@ -373,13 +373,13 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             float ey_new = 0.0f, ez_new = 0.0f;  // this lane's E^{n+1} y, z (for the x-face lanes)
             if constexpr (COMPACT) {
             const size_t i = (size_t)z * plane + col;
-            float rn0 = 0.0f, rn1 = 0.0f, rn2 = 0.0f;  // R^{n+1} (16-bit R: 0 where not updated)
+            float rho0 = 0.0f, rho1 = 0.0f, rho2 = 0.0f;  // 16-bit R: the residuals to store (0 where not updated)
             if (in_dom) {
                 const int t = ty * FTX + tx;
-                float r0, r1, r2;
+                float r0, r1, r2;    // R^n (32-bit R)
+                int q0, q1, q2;      // stored residuals and their segment's word (16-bit R)
+                uint32_t w;
                 if constexpr (R16) {
-                    int q0, q1, q2;
-                    uint32_t w;
                     if (TMA) {
                         const int16_t *T = reinterpret_cast<const int16_t *>(stage(k) + G::OFF_T);
                         constexpr int TS16 = pad128(G::T_BYTES) / 2;
@@ -393,9 +393,6 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                         q2 = reinterpret_cast<const int16_t *>(c.d_cur[2])[i];
                         w = c.r_exp[r16_word(c, z, bx, y)];
                     }
-                    r0 = r16_decode(q0, w, 0);
-                    r1 = r16_decode(q1, w, 1);
-                    r2 = r16_decode(q2, w, 2);
                 } else {
                     const float *T = reinterpret_cast<const float *>(stage(k) + G::OFF_T);
                     r0 = T[0 * TS + t];
@@ -429,11 +426,18 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     g1 = tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
                 // the per-cell test over the source list, in units that hold a
                 // source only, measured faster than the column mask in this form
-                // (which needs three more registers of the 48)
+                // (which needs three more registers of the 48); 16-bit R also
+                // needs the first matching entry (its FP32 R slot)
                 bool src = false;
-                if (unit_src)
-                    for (int s = 0; s < c.nsources; s++)
-                        src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
+                int src_at = -1;
+                if (unit_src) {
+                    for (int s = 0; s < c.nsources; s++) {
+                        const bool hit = c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
+                        src |= hit;
+                        if (R16 && hit && src_at < 0)
+                            src_at = s;
+                    }
+                }
                 if (dz_on || src) {
                     g2 = tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
                     if (src)
@@ -447,22 +451,43 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     const DebyeCoef kc = coef[min((int)cls, cls_max)];
                     const float k12 = kc.two_dt + kc.two_tau;
                     const int r = ty + 1, cc = tx + 4;
+                    if constexpr (R16) {  // R^n = rho - a E^n, or the source cell's FP32 R
+                        const float *rs = src_at >= 0 ? c.r_src + 3 * src_at : nullptr;
+                        r0 = rs ? rs[0] : fmaf(-kc.a, ea(0, r, cc), r16_decode(q0, w, 0));
+                        r1 = rs ? rs[1] : fmaf(-kc.a, ea(1, r, cc), r16_decode(q1, w, 1));
+                        r2 = rs ? rs[2] : fmaf(-kc.a, ea(2, r, cc), r16_decode(q2, w, 2));
+                    }
                     if (ex_on) {
                         const float e = ea(0, r, cc);
-                        c.e_prev[0][i] = kc.c * (kc.d * e + k12 * g0 + r0);
-                        rn0 = -kc.a * e - kc.two_tau * g0;
-                        if constexpr (!R16)
-                            c.d_prev[0][i] = rn0;
+                        const float en = kc.c * (kc.d * e + k12 * g0 + r0);
+                        const float rn = -kc.a * e - kc.two_tau * g0;
+                        c.e_prev[0][i] = en;
+                        if constexpr (R16) {
+                            if (src_at >= 0)
+                                c.r_src[3 * src_at] = rn;
+                            else
+                                rho0 = fmaf(kc.a, en, rn);
+                        } else {
+                            c.d_prev[0][i] = rn;
+                        }
                     }
                     if (eyz_on) {
                         const float e1 = ea(1, r, cc), e2 = ea(2, r, cc);
                         ey_new = kc.c * (kc.d * e1 + k12 * g1 + r1);
                         ez_new = kc.c * (kc.d * e2 + k12 * g2 + r2);
                         c.e_prev[1][i] = ey_new;
-                        rn1 = -kc.a * e1 - kc.two_tau * g1;
+                        const float rn1 = -kc.a * e1 - kc.two_tau * g1;
                         c.e_prev[2][i] = ez_new;
-                        rn2 = -kc.a * e2 - kc.two_tau * g2;
-                        if constexpr (!R16) {
+                        const float rn2 = -kc.a * e2 - kc.two_tau * g2;
+                        if constexpr (R16) {
+                            if (src_at >= 0) {
+                                c.r_src[3 * src_at + 1] = rn1;
+                                c.r_src[3 * src_at + 2] = rn2;
+                            } else {
+                                rho1 = fmaf(kc.a, ey_new, rn1);
+                                rho2 = fmaf(kc.a, ez_new, rn2);
+                            }
+                        } else {
                             c.d_prev[1][i] = rn1;
                             c.d_prev[2][i] = rn2;
                         }
@@ -471,11 +496,11 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             }
             if constexpr (R16) {
                 // every cell of the row segment is rewritten with the
-                // segment's new exponent (cells whose E is never updated
-                // keep R = 0, as in the 32-bit compact form)
+                // segment's new exponent (cells whose E is never updated,
+                // and source cells, store 0)
                 if (y < ny) {  // uniform over the warp: one warp is one row
                     uint32_t b0, b1, b2;
-                    const int q0 = r16_encode(rn0, b0), q1 = r16_encode(rn1, b1), q2 = r16_encode(rn2, b2);
+                    const int q0 = r16_encode(rho0, b0), q1 = r16_encode(rho1, b1), q2 = r16_encode(rho2, b2);
                     if (x < nx) {
                         reinterpret_cast<int16_t *>(c.d_prev[0])[i] = (int16_t)q0;
                         reinterpret_cast<int16_t *>(c.d_prev[1])[i] = (int16_t)q1;

@@ -297,13 +297,15 @@ enum {
      * stored: the D fields cannot be read, snapshotted or probed. */
     FDTD_KERNEL_COMPACT = 2,
     /* The compact form with R stored in 16 bits (no reference counterpart;
-     * the reduced-storage form): each R value is an int16 times a power of
-     * two shared by the 32 cells of one x-row segment of one plane (one
-     * exponent byte per component, the largest value of the segment keeps
-     * 15 significant bits).  H and E stay FP32 and all arithmetic is FP32;
-     * the step equals FDTD_KERNEL_COMPACT's with R rounded to that format
-     * after every step.  61.25 instead of 73 bytes of traffic per cell
-     * update.  D is not stored, as in FDTD_KERNEL_COMPACT. */
+     * the reduced-storage form).  Stored per cell and component is the
+     * residual rho = R^{n+1} + a E^{n+1} (a = 2 eps0 eps_inf tau), from
+     * which the next step recovers R with the FP32 E it reads; rho is an
+     * int16 times a power of two shared by the 32 cells of one x-row
+     * segment of one plane (one exponent byte per component: the largest
+     * residual of the segment keeps 15 significant bits).  Source cells keep
+     * R in FP32.  H and E stay FP32 and all arithmetic is FP32.  61.25
+     * instead of 73 bytes of traffic per cell update.  D is not stored, as
+     * in FDTD_KERNEL_COMPACT. */
     FDTD_KERNEL_COMPACT_R16 = 3
 };
 

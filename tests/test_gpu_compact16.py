@@ -44,10 +44,10 @@ def test_compact16_sphere_fields_and_probes_vs_fp64_oracle(cuda, tmp_path):
     The probes lie outside the source's row segments.  On the source row
     (y = z = 32, x = 0..63) the dipole's near field makes the 32-cell
     segments span more than three decades, and the segment's smaller cells
-    keep few bits of R: the probe at the sphere centre (32, 32, 32) is 0.3
-    off in relative L2 (0.22 when the same rounding is applied inside the
-    FP64 oracle) -- a limit of one exponent per segment, not met by this
-    form."""
+    keep few bits: the probe at the sphere centre (32, 32, 32), 16 cells
+    down that row, is off by about 1e-2 in relative L2 (the same rounding
+    applied inside the FP64 oracle gives 1.6e-2) -- a limit of one exponent
+    per segment, not met by this form."""
     p, codes, specs, s = _sphere(tmp_path, 64, 500, fg.KERNEL_COMPACT_R16)
     steps = p.iterationsCount
     probes = [(40, 30, 28), (24, 36, 34), (50, 50, 50), (32, 40, 32), (45, 20, 44)]
