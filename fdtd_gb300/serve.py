@@ -119,8 +119,8 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
     divide snapshot_every so snapshots land on exact step counts.  inputs
     (optional) maps request ids to build_inputs results that arrive with the
     requests; missing ones are built at admission.  kernel selects the state
-    form of every solve (KERNEL_SINGLE_PASS or KERNEL_COMPACT).  policy: the
-    admission order ("fifo" or "sjf", see order_queue).  max_active_cells
+    form of every solve (KERNEL_SINGLE_PASS, KERNEL_COMPACT or
+    KERNEL_COMPACT_R16).  policy: the admission order ("fifo" or "sjf", see order_queue).  max_active_cells
     (optional) caps the cells of the admitted solves: the batched launch
     needs only enough of them to fill the GPU, and admitting more only shares
     it among more requests, which lengthens every one; a request is admitted

@@ -24,6 +24,7 @@ class Recorder:
 
 
 @pytest.mark.parametrize("kernel,policy", [(fg.KERNEL_SINGLE_PASS, "fifo"), (fg.KERNEL_COMPACT, "fifo"),
+                                           (fg.KERNEL_COMPACT_R16, "fifo"),
                                            (fg.KERNEL_COMPACT, "sjf")])
 def test_served_results_equal_lone_runs_and_overlap(cuda, tmp_path, kernel, policy):
     reqs = serve.poisson_stream(rate=40.0, duration=0.3, seed=3, dims=(24, 56), steps=(50, 150))
