@@ -43,7 +43,7 @@ SCHEME_CORRECTED = 1
 KERNEL_SINGLE_PASS = 0
 KERNEL_TWO_PASS = 1
 KERNEL_COMPACT = 2      # nine stored fields (H, E, R); D is not readable
-KERNEL_COMPACT_R16 = 3  # the same with R in 16 bits (int16 + one exponent per 32-cell row segment)
+KERNEL_COMPACT_R16 = 3  # the same with R in 16 bits (FP16 residual + one scale per 32-cell row segment)
 COMPACT_KERNELS = (KERNEL_COMPACT, KERNEL_COMPACT_R16)
 FIELDS = ("hx", "hy", "hz", "dx", "dy", "dz", "ex", "ey", "ez")
 FIELD_ID = {n: i for i, n in enumerate(FIELDS)}

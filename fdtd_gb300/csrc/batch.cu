@@ -1,8 +1,8 @@
 // batch.cu -- many independent solves of uneven sizes advanced together.
 //
 // Each solve keeps its own resident state (H x2, E x2, D x2 or, in a batch of
-// the compact form, R x1 -- int16 R and its exponent words in the 16-bit
-// form -- and the classes) with
+// the compact form, R x1 -- FP16 residuals and their exponent words in the
+// 16-bit form -- and the classes) with
 // rows padded to a multiple of 16 cells, so every solve gets TMA staging, and
 // its own plan (class table, source table, Mur slabs) and step counter.  A
 // batched step is three launches: one persistent kernel over the work units
@@ -38,20 +38,19 @@ struct BatchSolve {
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
     uint32_t *rexp = nullptr;  // 16-bit R form: exponent words
-    float *rsrc = nullptr;     // ... and the source cells' FP32 R
     int *counter = nullptr;
 };
 
 size_t padded_pitch(int nx) { return ((size_t)nx + 15) & ~size_t(15); }
 
-size_t r16_array_bytes(size_t ncell) { return (ncell * sizeof(int16_t) + 255) & ~size_t(255); }
+size_t r16_array_bytes(size_t ncell) { return (ncell * sizeof(uint16_t) + 255) & ~size_t(255); }
 size_t r16_exp_bytes(int nx, int ny, int nz) { return (r16_words(nx, ny, nz) * sizeof(uint32_t) + 255) & ~size_t(255); }
 
 size_t state_bytes(int nx, int ny, int nz, bool compact, bool r16 = false)
 {
     const size_t ncell = padded_pitch(nx) * ny * nz;
     const size_t f = (ncell * sizeof(float) + 255) & ~size_t(255);
-    const size_t d = r16 ? 3 * r16_array_bytes(ncell) + r16_exp_bytes(nx, ny, nz) + 256 : (compact ? 3 : 6) * f;
+    const size_t d = r16 ? 3 * r16_array_bytes(ncell) + r16_exp_bytes(nx, ny, nz) : (compact ? 3 : 6) * f;
     return 12 * f + d + ((ncell + 255) & ~size_t(255)) + 256;
 }
 
@@ -118,7 +117,6 @@ NativeConsts solve_consts(const BatchSolve *v, int parity)
     c.pitch = v->pitch;
     c.step_counter = v->counter;
     c.r_exp = v->rexp;
-    c.r_src = v->rsrc;
     return c;
 }
 
@@ -357,8 +355,6 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         if (b->r16) {
             v->rexp = reinterpret_cast<uint32_t *>(q);
             q += r16_exp_bytes(p->nx, p->ny, p->nz);
-            v->rsrc = reinterpret_cast<float *>(q);
-            q += 256;  // R16_SRC_FLOATS floats
         }
         v->mat = reinterpret_cast<uint8_t *>(q);
         q += (v->ncell + 255) & ~size_t(255);

@@ -56,8 +56,7 @@ struct NativeConsts {
                            // kernel of the same step skips them (set for both launches or neither)
     const float4 *mur_x;   // per x-face cell: 1/(dt+q_self), dt-q_nbr, dt+q_nbr, dt-q_self, [face][z][y]
     uint32_t *r_exp;       // compact form with 16-bit R: the segment exponent words (see r16_words),
-                           // and d_cur == d_prev hold int16 values; null in the other forms
-    float *r_src;          // ... and R of the source cells in FP32, 3 per source (R16_SRC_FLOATS)
+                           // and d_cur == d_prev hold the FP16 residuals; null in the other forms
     const float *h_in[3];
     float *h_out[3];
     const float *e_cur[3];
@@ -94,20 +93,19 @@ int launch_step(const NativeConsts &c, cudaStream_t s);
 // rho_k = R_k^{n+1} + a E_k^{n+1} (a = 2 eps0 eps_inf tau of the cell's
 // class), which the next step turns back into R_k = rho_k - a E_k with the
 // FP32 E it reads anyway; rho is a few percent of R where the field varies
-// over many steps.  rho_k is an int16 q times 2^(b - 127), where b (1..254) is
-// shared by the 32 cells x0 .. x0+31 of one row of one plane (x0 a multiple
-// of 32) and held in byte k of that row segment's exponent word.  Words are
-// laid out [z][x / 32][y] with each segment's column padded to r16_rows(ny)
-// words (TMA stages a tile's 8 rows as one 32-byte box).  An all-zero word
-// decodes to 0.  Source cells keep R in FP32 outside the blocks (r_src), so
-// the injected current does not set their segment's exponent.
+// over many steps.  rho_k is an FP16 value h times 2^(b - 127), where b
+// (1..254) is shared by the 32 cells x0 .. x0+31 of one row of one plane (x0
+// a multiple of 32) and held in byte k of that row segment's exponent word;
+// b puts the segment's largest |rho_k| in [2^14, 2^15), so every value keeps
+// FP16's 11 significant bits down to 2^-29 of it.  Words are laid out
+// [z][x / 32][y] with each segment's column padded to r16_rows(ny) words (TMA
+// stages a tile's 8 rows as one 32-byte box).  An all-zero word decodes to 0.
 __host__ __device__ inline int r16_segments(int nx) { return (nx + 31) / 32; }
 __host__ __device__ inline int r16_rows(int ny) { return (ny + 7) & ~7; }
 __host__ __device__ inline size_t r16_words(int nx, int ny, int nz)
 {
     return (size_t)nz * r16_segments(nx) * r16_rows(ny);
 }
-constexpr int R16_SRC_FLOATS = 3 * FDTD_MAX_SOURCES;
 // Compact nine-field step (d_cur == d_prev == R, updated in place) + Mur.
 int launch_step_compact(const NativeConsts &c, cudaStream_t s);
 int launch_h_e_compact(const NativeConsts &c, cudaStream_t s);

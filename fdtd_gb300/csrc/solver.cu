@@ -47,7 +47,6 @@ NativeConsts solver_consts(const fdtd_solver *s, int n)
     const fdtd_native_fields f = step_fields(s, n);
     NativeConsts c = make_consts(s->plan, &f, n);
     c.r_exp = s->rexp;
-    c.r_src = s->rsrc;
     return c;
 }
 
@@ -335,17 +334,15 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         return st;
     }
     // H: two buffers for the single-pass kernels, one for the two-pass pair;
-    // E: two slots; D: two slots, or one R array for the compact form (int16
-    // R and its exponent words for the 16-bit form)
+    // E: two slots; D: two slots, or one R array for the compact form (FP16
+    // residuals and their exponent words for the 16-bit form)
     const bool r16 = cfg->kernel == FDTD_KERNEL_COMPACT_R16;
     const int nh = cfg->kernel == FDTD_KERNEL_TWO_PASS ? 1 : 2;
     const int nd = stores_no_d(cfg->kernel) ? 1 : 2;
     const size_t fbytes = ((n * sizeof(float)) + 255) & ~size_t(255);
-    const size_t dbytes = r16 ? ((n * sizeof(int16_t)) + 255) & ~size_t(255) : fbytes;
+    const size_t dbytes = r16 ? ((n * sizeof(uint16_t)) + 255) & ~size_t(255) : fbytes;
     const size_t xbytes = r16 ? ((r16_words(p->nx, p->ny, p->nz) * sizeof(uint32_t)) + 255) & ~size_t(255) : 0;
-    const size_t sbytes = r16 ? 256 : 0;  // R16_SRC_FLOATS floats
-    static_assert(R16_SRC_FLOATS * sizeof(float) <= 256, "source R slots fit 256 bytes");
-    const size_t total = fbytes * (3 * nh + 6) + dbytes * 3 * nd + xbytes + sbytes + ((n + 255) & ~size_t(255)) + 256;
+    const size_t total = fbytes * (3 * nh + 6) + dbytes * 3 * nd + xbytes + ((n + 255) & ~size_t(255)) + 256;
     st = cu(cudaMalloc(&s->d_block, total));
     if (st == FDTD_OK) {
         char *q = s->d_block;
@@ -367,8 +364,6 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         if (r16) {
             s->rexp = reinterpret_cast<uint32_t *>(q);
             q += xbytes;
-            s->rsrc = reinterpret_cast<float *>(q);
-            q += sbytes;
         }
         s->mat = reinterpret_cast<uint8_t *>(q);
         q += (n + 255) & ~size_t(255);

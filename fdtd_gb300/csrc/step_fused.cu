@@ -40,8 +40,8 @@ static_assert(FTX == FUSED_TILE_X, "x-face Mur fusion assumes 32-column tiles");
 
 // Shared-memory layout of one stage for NT tile arrays of TB-byte elements
 // (9 floats: D^n, D^{n-1}, E^{n-1} of the D form; 3 floats: R of the compact
-// form; 3 int16: R of the compact form with 16-bit R, which also stages its
-// TY exponent words, XB bytes).
+// form; 3 FP16 residuals of the compact form with 16-bit R, which also
+// stages its TY exponent words, XB bytes).
 template <int TY, int NT = 9, int TB = 4, int XB = 0>
 struct Geo {
     static constexpr int EW = FTX + 8, EH = TY + 2;   // E^n box: x0-4 .. x0+TX+3, y0-1 .. y0+TY
@@ -154,27 +154,31 @@ __device__ __forceinline__ size_t r16_word(const NativeConsts &c, int z, int bx,
     return ((size_t)z * r16_segments(c.nx) + bx) * r16_rows(c.ny) + y;
 }
 
-// R_k of a cell from its int16 value q and its segment's word w (exact:
-// q has at most 16 significant bits and 2^(b-127) is a normal float; w = 0
-// gives 0).
-__device__ __forceinline__ float r16_decode(int q, uint32_t w, int k)
+// The residual of a cell from its stored FP16 bits h and its segment's word
+// w: h times 2^(b - 127), b the word's byte k (exact: an FP16 value has 11
+// significant bits and 2^(b-127) is a normal float; w = 0 gives 0).
+__device__ __forceinline__ float r16_decode(unsigned short h, uint32_t w, int k)
 {
-    return __int2float_rn(q) * __uint_as_float(((w >> (8 * k)) & 0xffu) << 23);
+    float f;
+    asm("cvt.f32.f16 %0, %1;" : "=f"(f) : "h"(h));
+    return f * __uint_as_float(((w >> (8 * k)) & 0xffu) << 23);
 }
 
 // Warp-collective (every lane of the warp calls it; one warp is one row
 // segment): b = e - 14, at least 1, for the largest |r| of the segment with
-// biased exponent e, and this lane's q = round-to-nearest-even(r 2^(127-b))
-// saturated to int16.  The largest value keeps 15 significant bits; the
-// scaling by a power of two is exact.  Lanes outside the grid pass r = 0.
-__device__ __forceinline__ int r16_encode(float r, uint32_t &b)
+// biased exponent e, and this lane's FP16 bits of r 2^(127-b) rounded to
+// nearest even.  The scaling by a power of two is exact and puts the
+// segment's largest value in [2^14, 2^15), below the FP16 maximum; every
+// value above 2^-29 of it keeps FP16's 11 significant bits.  Lanes outside
+// the grid pass r = 0.
+__device__ __forceinline__ unsigned short r16_encode(float r, uint32_t &b)
 {
     const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(r) & 0x7fffffffu);
     b = (unsigned)max((int)(m >> 23) - 14, 1);
     const float v = r * __uint_as_float((254u - b) << 23);
-    short q;
-    asm("cvt.rni.sat.s16.f32 %0, %1;" : "=h"(q) : "f"(v));
-    return q;
+    unsigned short h;
+    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h) : "f"(v));
+    return h;
 }
 
 // One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
@@ -377,20 +381,20 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             if (in_dom) {
                 const int t = ty * FTX + tx;
                 float r0, r1, r2;    // R^n (32-bit R)
-                int q0, q1, q2;      // stored residuals and their segment's word (16-bit R)
+                unsigned short q0, q1, q2;  // stored residuals (FP16 bits) and their segment's word (16-bit R)
                 uint32_t w;
                 if constexpr (R16) {
                     if (TMA) {
-                        const int16_t *T = reinterpret_cast<const int16_t *>(stage(k) + G::OFF_T);
+                        const unsigned short *T = reinterpret_cast<const unsigned short *>(stage(k) + G::OFF_T);
                         constexpr int TS16 = pad128(G::T_BYTES) / 2;
                         q0 = T[t];
                         q1 = T[TS16 + t];
                         q2 = T[2 * TS16 + t];
                         w = reinterpret_cast<const uint32_t *>(stage(k) + G::OFF_X)[ty];
                     } else {
-                        q0 = reinterpret_cast<const int16_t *>(c.d_cur[0])[i];
-                        q1 = reinterpret_cast<const int16_t *>(c.d_cur[1])[i];
-                        q2 = reinterpret_cast<const int16_t *>(c.d_cur[2])[i];
+                        q0 = reinterpret_cast<const unsigned short *>(c.d_cur[0])[i];
+                        q1 = reinterpret_cast<const unsigned short *>(c.d_cur[1])[i];
+                        q2 = reinterpret_cast<const unsigned short *>(c.d_cur[2])[i];
                         w = c.r_exp[r16_word(c, z, bx, y)];
                     }
                 } else {
@@ -426,18 +430,11 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     g1 = tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
                 // the per-cell test over the source list, in units that hold a
                 // source only, measured faster than the column mask in this form
-                // (which needs three more registers of the 48); 16-bit R also
-                // needs the first matching entry (its FP32 R slot)
+                // (which needs three more registers of the 48)
                 bool src = false;
-                int src_at = -1;
-                if (unit_src) {
-                    for (int s = 0; s < c.nsources; s++) {
-                        const bool hit = c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
-                        src |= hit;
-                        if (R16 && hit && src_at < 0)
-                            src_at = s;
-                    }
-                }
+                if (unit_src)
+                    for (int s = 0; s < c.nsources; s++)
+                        src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
                 if (dz_on || src) {
                     g2 = tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
                     if (src)
@@ -451,11 +448,10 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     const DebyeCoef kc = coef[min((int)cls, cls_max)];
                     const float k12 = kc.two_dt + kc.two_tau;
                     const int r = ty + 1, cc = tx + 4;
-                    if constexpr (R16) {  // R^n = rho - a E^n, or the source cell's FP32 R
-                        const float *rs = src_at >= 0 ? c.r_src + 3 * src_at : nullptr;
-                        r0 = rs ? rs[0] : fmaf(-kc.a, ea(0, r, cc), r16_decode(q0, w, 0));
-                        r1 = rs ? rs[1] : fmaf(-kc.a, ea(1, r, cc), r16_decode(q1, w, 1));
-                        r2 = rs ? rs[2] : fmaf(-kc.a, ea(2, r, cc), r16_decode(q2, w, 2));
+                    if constexpr (R16) {  // R^n = rho - a E^n
+                        r0 = fmaf(-kc.a, ea(0, r, cc), r16_decode(q0, w, 0));
+                        r1 = fmaf(-kc.a, ea(1, r, cc), r16_decode(q1, w, 1));
+                        r2 = fmaf(-kc.a, ea(2, r, cc), r16_decode(q2, w, 2));
                     }
                     if (ex_on) {
                         const float e = ea(0, r, cc);
@@ -463,10 +459,7 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                         const float rn = -kc.a * e - kc.two_tau * g0;
                         c.e_prev[0][i] = en;
                         if constexpr (R16) {
-                            if (src_at >= 0)
-                                c.r_src[3 * src_at] = rn;
-                            else
-                                rho0 = fmaf(kc.a, en, rn);
+                            rho0 = fmaf(kc.a, en, rn);
                         } else {
                             c.d_prev[0][i] = rn;
                         }
@@ -480,13 +473,8 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                         c.e_prev[2][i] = ez_new;
                         const float rn2 = -kc.a * e2 - kc.two_tau * g2;
                         if constexpr (R16) {
-                            if (src_at >= 0) {
-                                c.r_src[3 * src_at + 1] = rn1;
-                                c.r_src[3 * src_at + 2] = rn2;
-                            } else {
-                                rho1 = fmaf(kc.a, ey_new, rn1);
-                                rho2 = fmaf(kc.a, ez_new, rn2);
-                            }
+                            rho1 = fmaf(kc.a, ey_new, rn1);
+                            rho2 = fmaf(kc.a, ez_new, rn2);
                         } else {
                             c.d_prev[1][i] = rn1;
                             c.d_prev[2][i] = rn2;
@@ -496,15 +484,16 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             }
             if constexpr (R16) {
                 // every cell of the row segment is rewritten with the
-                // segment's new exponent (cells whose E is never updated,
-                // and source cells, store 0)
+                // segment's new exponent (cells whose E is never updated
+                // store 0)
                 if (y < ny) {  // uniform over the warp: one warp is one row
                     uint32_t b0, b1, b2;
-                    const int q0 = r16_encode(rho0, b0), q1 = r16_encode(rho1, b1), q2 = r16_encode(rho2, b2);
+                    const unsigned short h0 = r16_encode(rho0, b0), h1 = r16_encode(rho1, b1),
+                                         h2 = r16_encode(rho2, b2);
                     if (x < nx) {
-                        reinterpret_cast<int16_t *>(c.d_prev[0])[i] = (int16_t)q0;
-                        reinterpret_cast<int16_t *>(c.d_prev[1])[i] = (int16_t)q1;
-                        reinterpret_cast<int16_t *>(c.d_prev[2])[i] = (int16_t)q2;
+                        reinterpret_cast<unsigned short *>(c.d_prev[0])[i] = h0;
+                        reinterpret_cast<unsigned short *>(c.d_prev[1])[i] = h1;
+                        reinterpret_cast<unsigned short *>(c.d_prev[2])[i] = h2;
                     }
                     if (tx == 0)
                         c.r_exp[r16_word(c, z, bx, y)] = b0 | (b1 << 8) | (b2 << 16);
@@ -879,7 +868,7 @@ bool fused_uses_tma(const NativeConsts &c)
 
 // Tensor maps of one step: E^n and H^{n-1/2} halo boxes (0-5), the tile
 // arrays (D form: D^n, D^{n-1}, E^{n-1} at 6-14; compact form: R at 6-8) and
-// the class volume after them; with 16-bit R (int16 tiles at 6-8) the
+// the class volume after them; with 16-bit R (FP16 tiles at 6-8) the
 // exponent words at 10 (box: one segment's TY rows).
 bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps, bool r16)
 {

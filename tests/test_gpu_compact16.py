@@ -1,7 +1,8 @@
 """Compact form with R stored in 16 bits (FDTD_KERNEL_COMPACT_R16): the
 compact form's update (updateEField, fdtd_calculations.cu:141-183, with D and
-E^{n-1} folded into R) with R held as an int16 per cell and one exponent byte
-per component per 32-cell row segment.  H, E and the arithmetic stay FP32, so
+E^{n-1} folded into R) with the residual R^{n+1} + a E^{n+1} held as an FP16
+value per cell and one power-of-two scale byte per component per 32-cell
+row segment.  H, E and the arithmetic stay FP32, so
 the form is judged against the FP64 oracle at the reduced-storage tolerance
 R16_TOL (relative L2 of each E field and of each probe's E series; H, the
 curl of E, at R16_H_TOL), and against the 32-bit compact form."""
@@ -39,18 +40,15 @@ def _sphere(root, n, t_max, kernel, timeskip=0.99):
 
 def test_compact16_sphere_fields_and_probes_vs_fp64_oracle(cuda, tmp_path):
     """64^3 Debye sphere, dt = 0.99 of the Courant limit, 501 steps: E and H
-    and the E series at probes inside and outside the sphere.
-
-    The probes lie outside the source's row segments.  On the source row
-    (y = z = 32, x = 0..63) the dipole's near field makes the 32-cell
-    segments span more than three decades, and the segment's smaller cells
-    keep few bits: the probe at the sphere centre (32, 32, 32), 16 cells
-    down that row, is off by about 1e-2 in relative L2 (the same rounding
-    applied inside the FP64 oracle gives 1.6e-2) -- a limit of one exponent
-    per segment, not met by this form."""
+    and the E series at probes inside and outside the sphere, among them
+    cells on the source's row (y = z = 32), where the dipole's near field
+    makes one 32-cell segment span more than three decades: FP16 keeps 11
+    significant bits for every value of a segment, so the small ones there
+    lose nothing to the segment's scale."""
     p, codes, specs, s = _sphere(tmp_path, 64, 500, fg.KERNEL_COMPACT_R16)
     steps = p.iterationsCount
-    probes = [(40, 30, 28), (24, 36, 34), (50, 50, 50), (32, 40, 32), (45, 20, 44)]
+    probes = [(32, 32, 32), (20, 32, 32), (31, 32, 32), (40, 30, 28), (24, 36, 34), (50, 50, 50), (32, 40, 32),
+              (45, 20, 44)]
     s.set_probes(probes, capacity=steps)
     s.run(steps)
     got = s.fields()
@@ -126,7 +124,7 @@ def test_compact16_has_no_d_fields_and_zero_steps_stay_zero(cuda, tmp_path):
 
 @pytest.mark.parametrize("at", [0, 13])
 def test_compact16_checkpoint_resume_is_bit_identical(cuda, tmp_path, at):
-    """The checkpoint holds the int16 R and its exponent words as stored."""
+    """The checkpoint holds the FP16 residuals and their exponent words as stored."""
     p, codes, specs, a = _sphere(tmp_path / "a", 32, 60, fg.KERNEL_COMPACT_R16)
     a.run(at)
     a.checkpoint(tmp_path / "ck.bin")
