@@ -133,9 +133,7 @@ def test_compact16_batch_matches_lone_solves_and_oracle(cuda):
             alone = s.fields()
         for name in got:
             assert np.array_equal(got[name].view(np.uint32), alone[name].view(np.uint32)), (dims, name)
-        want = _oracle(*case)
-        assert_fields_close(got, want, tol=1e-3, names=["ex", "ey", "ez"])
-        assert_fields_close(got, want, tol=5e-3, names=["hx", "hy", "hz"])
+        assert_fields_close(got, _oracle(*case), tol=1e-3, names=list(got))
     b.close()
 
 
