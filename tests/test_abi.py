@@ -54,3 +54,12 @@ def test_drop_in_executable_built_and_reports_usage():
     assert r.returncode == 2 and "usage" in r.stderr
     r = subprocess.run([str(fg.EXE_PATH), "--params", "/nonexistent/input_params"], capture_output=True, text=True)
     assert r.returncode == 1 and "failed" in r.stderr
+
+
+def test_kernel_form_ids_match_the_header():
+    """The Python mirror's form ids are the header's enum values."""
+    text = (HEADER_DIR / "fdtd_gb300.h").read_text()
+    ids = {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(FDTD_KERNEL_[A-Z0-9_]+)\s*=\s*(\d+)", text)}
+    assert ids == {"FDTD_KERNEL_SINGLE_PASS": fg.KERNEL_SINGLE_PASS, "FDTD_KERNEL_TWO_PASS": fg.KERNEL_TWO_PASS,
+                   "FDTD_KERNEL_COMPACT": fg.KERNEL_COMPACT, "FDTD_KERNEL_COMPACT_R16": fg.KERNEL_COMPACT_R16}
+    assert set(fg.COMPACT_KERNELS) == {fg.KERNEL_COMPACT, fg.KERNEL_COMPACT_R16}
