@@ -43,7 +43,7 @@ B_ALG = 97  # bytes per cell-update: 15 state floats read, 9 written, 1-byte cla
 KERNEL_BYTES = {
     "fused_step": 97,    # H, E^n, E^{n-1}, D^n, D^{n-1} read; H, E, D written; class
     "compact_step": 73,  # H, E^n, R read; H, E, R written; class
-    # H, E^n read and written as floats, R as an FP16 residual, one 4-byte exponent word per 32 cells, class
+    # H, E^n read and written as floats, R as an FP16 residual, one 4-byte scale word per 32 cells, class
     "compact16_step": 61.25,
     "de": 85,            # H, E^n, E^{n-1}, D^n, D^{n-1} read; E, D written; class
     "h": 36,             # H, E read; H written
@@ -56,8 +56,8 @@ STATE_BYTES = {"single": 73, "two_pass": 61, "compact": 61, "compact16": 55.125}
 FORM_STATE = {
     "compact": "H (2 buffers), E (2 slots), R = -a E^{n-1} - 2 tau (D^n - D^{n-1}); D not stored",
     "compact16": "as compact, R stored as the residual R + a E^{n+1} in FP16 with one power-of-two scale "
-                 "byte per component per 32-cell row segment (11 significant bits for every value); FP32 "
-                 "arithmetic; D not stored",
+                 "per 32-cell row segment shared by the three components (11 significant bits for every "
+                 "value); FP32 arithmetic; D not stored",
 }
 PRECISION_PROBES = 16
 PRECISION_SEED = 2024

@@ -1,7 +1,7 @@
 // batch.cu -- many independent solves of uneven sizes advanced together.
 //
 // Each solve keeps its own resident state (H x2, E x2, D x2 or, in a batch of
-// the compact form, R x1 -- FP16 residuals and their exponent words in the
+// the compact form, R x1 -- FP16 residuals and their scale words in the
 // 16-bit form -- and the classes) with
 // rows padded to a multiple of 16 cells, so every solve gets TMA staging, and
 // its own plan (class table, source table, Mur slabs) and step counter.  A
@@ -37,7 +37,7 @@ struct BatchSolve {
     float *e[2][3] = {};
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
-    uint32_t *rexp = nullptr;  // 16-bit R form: exponent words
+    uint32_t *rexp = nullptr;  // 16-bit R form: scale words
     int *counter = nullptr;
 };
 

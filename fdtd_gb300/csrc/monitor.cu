@@ -321,14 +321,14 @@ static const char CKP_MAGIC[8] = {'F', 'D', 'T', 'D', 'G', 'B', '3', 'C'};
 
 // Checkpoint versions: 1 holds the D form's 15 arrays (either D-form
 // kernel restores it), 2 the compact form's 12, 3 the 16-bit-R form's 9
-// float arrays, its three FP16 residual arrays and its exponent words.
+// float arrays, its three FP16 residual arrays and its scale words.
 static uint32_t ckp_version(const fdtd_solver *s)
 {
     return s->kernel == FDTD_KERNEL_COMPACT_R16 ? 3u : s->kernel == FDTD_KERNEL_COMPACT ? 2u : 1u;
 }
 
 // The state blocks after `count` steps: H, E^n, E^{n-1}, then D^n, D^{n-1}
-// (D form), R (compact form) or the FP16 residuals and the exponent words.
+// (D form), R (compact form) or the FP16 residuals and the scale words.
 static int state_blocks(fdtd_solver *s, int count, void *ptr[16], size_t bytes[16])
 {
     const int hb = s->kernel != FDTD_KERNEL_TWO_PASS ? (count & 1) : 0;

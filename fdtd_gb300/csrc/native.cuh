@@ -55,7 +55,7 @@ struct NativeConsts {
     int fuse_mur_x;        // the single-pass kernel applies the x-face Mur updates and the Mur
                            // kernel of the same step skips them (set for both launches or neither)
     const float4 *mur_x;   // per x-face cell: 1/(dt+q_self), dt-q_nbr, dt+q_nbr, dt-q_self, [face][z][y]
-    uint32_t *r_exp;       // compact form with 16-bit R: the segment exponent words (see r16_words),
+    uint32_t *r_exp;       // compact form with 16-bit R: the segment scale words (see r16_words),
                            // and d_cur == d_prev hold the FP16 residuals; null in the other forms
     const float *h_in[3];
     float *h_out[3];
@@ -94,12 +94,13 @@ int launch_step(const NativeConsts &c, cudaStream_t s);
 // class), which the next step turns back into R_k = rho_k - a E_k with the
 // FP32 E it reads anyway; rho is a few percent of R where the field varies
 // over many steps.  rho_k is an FP16 value h times 2^(b - 127), where b
-// (1..254) is shared by the 32 cells x0 .. x0+31 of one row of one plane (x0
-// a multiple of 32) and held in byte k of that row segment's exponent word;
-// b puts the segment's largest |rho_k| in [2^14, 2^15), so every value keeps
-// FP16's 11 significant bits down to 2^-29 of it.  Words are laid out
-// [z][x / 32][y] with each segment's column padded to r16_rows(ny) words (TMA
-// stages a tile's 8 rows as one 32-byte box).  An all-zero word decodes to 0.
+// (1..254) is shared by the three components of the 32 cells x0 .. x0+31 of
+// one row of one plane (x0 a multiple of 32) and held in the low byte of that
+// row segment's scale word; b puts the segment's largest |rho| in [2^14,
+// 2^15), so every value keeps FP16's 11 significant bits down to 2^-29 of it.
+// Words are laid out [z][x / 32][y] with each segment's column padded to
+// r16_rows(ny) words (TMA stages a tile's 8 rows as one 32-byte box).  An
+// all-zero word decodes to 0.
 __host__ __device__ inline int r16_segments(int nx) { return (nx + 31) / 32; }
 __host__ __device__ inline int r16_rows(int ny) { return (ny + 7) & ~7; }
 __host__ __device__ inline size_t r16_words(int nx, int ny, int nz)

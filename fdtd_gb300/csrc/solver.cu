@@ -335,7 +335,7 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     }
     // H: two buffers for the single-pass kernels, one for the two-pass pair;
     // E: two slots; D: two slots, or one R array for the compact form (FP16
-    // residuals and their exponent words for the 16-bit form)
+    // residuals and their scale words for the 16-bit form)
     const bool r16 = cfg->kernel == FDTD_KERNEL_COMPACT_R16;
     const int nh = cfg->kernel == FDTD_KERNEL_TWO_PASS ? 1 : 2;
     const int nd = stores_no_d(cfg->kernel) ? 1 : 2;

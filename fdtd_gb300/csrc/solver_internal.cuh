@@ -34,7 +34,7 @@ struct fdtd_solver {
     float *e[2][3] = {};
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
-    uint32_t *rexp = nullptr;  // FDTD_KERNEL_COMPACT_R16: exponent words (d[0] holds the FP16 residuals)
+    uint32_t *rexp = nullptr;  // FDTD_KERNEL_COMPACT_R16: scale words (d[0] holds the FP16 residuals)
     int *counter = nullptr;
     int steps = 0;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (parity, length) -> exec

@@ -41,7 +41,7 @@ static_assert(FTX == FUSED_TILE_X, "x-face Mur fusion assumes 32-column tiles");
 // Shared-memory layout of one stage for NT tile arrays of TB-byte elements
 // (9 floats: D^n, D^{n-1}, E^{n-1} of the D form; 3 floats: R of the compact
 // form; 3 FP16 residuals of the compact form with 16-bit R, which also
-// stages its TY exponent words, XB bytes).
+// stages its TY scale words, XB bytes).
 template <int TY, int NT = 9, int TB = 4, int XB = 0>
 struct Geo {
     static constexpr int EW = FTX + 8, EH = TY + 2;   // E^n box: x0-4 .. x0+TX+3, y0-1 .. y0+TY
@@ -73,7 +73,7 @@ struct FusedArgs {
 // TMA: one thread arms the stage's barrier and issues the plane's boxes.
 // With arm_only (the stall test hook) the barrier expects the plane's bytes
 // but no copy is issued.  The tile maps follow the six halo maps, then the
-// classes, then (16-bit R) the exponent words.
+// classes, then (16-bit R) the scale words.
 template <int TY, int NT = 9, int TB = 4, int XB = 0>
 __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uint32_t bar, int kind, int x0, int y0,
                                 int z, bool arm_only = false)
@@ -94,13 +94,13 @@ __device__ void issue_plane_tma(const FusedMaps &maps, unsigned char *stage, uin
     for (int k = 0; k < NT; k++)
         tma_load_3d(smem_addr(stage + G::OFF_T + k * pad128(G::T_BYTES)), &maps.m[6 + k], x0, y0, z, bar);
     tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[6 + NT], x0, y0, z, bar);
-    if (XB > 0)  // exponent words of rows y0 .. y0+TY-1 of segment x0 / 32 (y0 * 4 bytes: 16-byte aligned)
+    if (XB > 0)  // scale words of rows y0 .. y0+TY-1 of segment x0 / 32 (y0 * 4 bytes: 16-byte aligned)
         tma_load_3d(smem_addr(stage + G::OFF_X), &maps.m[7 + NT], y0, x0 / FTX, z, bar);
 }
 
 // Generic: every thread copies part of each box with 4-byte cp.async
 // (zero-filled outside the grid); the material classes are read separately,
-// and so are 16-bit R and its exponent words (no tiles staged for them).
+// and so are 16-bit R and its scale words (no tiles staged for them).
 template <int TY, int NT = 9, int TB = 4, int XB = 0>
 __device__ void issue_plane_generic(const NativeConsts &c, unsigned char *stage, int kind, int x0, int y0, int z,
                                     int tid)
@@ -148,37 +148,45 @@ __device__ __forceinline__ bool unit_has_source(const NativeConsts &c, int x0, i
 
 // ---- 16-bit R (layout: r16_segments / r16_rows / r16_words)
 
-// Index of the exponent word of row y, segment bx, plane z.
+// Index of the scale word of row y, segment bx, plane z.
 __device__ __forceinline__ size_t r16_word(const NativeConsts &c, int z, int bx, int y)
 {
     return ((size_t)z * r16_segments(c.nx) + bx) * r16_rows(c.ny) + y;
 }
 
-// The residual of a cell from its stored FP16 bits h and its segment's word
-// w: h times 2^(b - 127), b the word's byte k (exact: an FP16 value has 11
-// significant bits and 2^(b-127) is a normal float; w = 0 gives 0).
-__device__ __forceinline__ float r16_decode(unsigned short h, uint32_t w, int k)
+// The scale 2^(b - 127) of a segment's word w (b in its low byte; w = 0
+// gives 0).
+__device__ __forceinline__ float r16_scale(uint32_t w) { return __uint_as_float(w << 23); }
+
+// The residual of a cell from its stored FP16 bits h and its segment's
+// scale (exact: an FP16 value has 11 significant bits and the scale is a
+// normal power of two).
+__device__ __forceinline__ float r16_decode(unsigned short h, float scale)
 {
     float f;
     asm("cvt.f32.f16 %0, %1;" : "=f"(f) : "h"(h));
-    return f * __uint_as_float(((w >> (8 * k)) & 0xffu) << 23);
+    return f * scale;
 }
 
 // Warp-collective (every lane of the warp calls it; one warp is one row
-// segment): b = e - 14, at least 1, for the largest |r| of the segment with
-// biased exponent e, and this lane's FP16 bits of r 2^(127-b) rounded to
-// nearest even.  The scaling by a power of two is exact and puts the
-// segment's largest value in [2^14, 2^15), below the FP16 maximum; every
-// value above 2^-29 of it keeps FP16's 11 significant bits.  Lanes outside
-// the grid pass r = 0.
-__device__ __forceinline__ unsigned short r16_encode(float r, uint32_t &b)
+// segment): b = e - 14, at least 1, for the largest |r0|, |r1|, |r2| of the
+// segment with biased exponent e; returns b and sets each hk to the FP16
+// bits of rk 2^(127-b) rounded to nearest even.  The scaling by a power of
+// two is exact and puts the segment's largest value in [2^14, 2^15), below
+// the FP16 maximum; every value above 2^-29 of it keeps FP16's 11
+// significant bits, so the three components share one scale.  Lanes
+// outside the grid pass zeros.
+__device__ __forceinline__ uint32_t r16_encode(float r0, float r1, float r2, unsigned short &h0, unsigned short &h1,
+                                               unsigned short &h2)
 {
-    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(r) & 0x7fffffffu);
-    b = (unsigned)max((int)(m >> 23) - 14, 1);
-    const float v = r * __uint_as_float((254u - b) << 23);
-    unsigned short h;
-    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h) : "f"(v));
-    return h;
+    const float a = fmaxf(fmaxf(fabsf(r0), fabsf(r1)), fabsf(r2));
+    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(a));
+    const uint32_t b = (uint32_t)max((int)(m >> 23) - 14, 1);
+    const float mult = __uint_as_float((254u - b) << 23);
+    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h0) : "f"(r0 * mult));
+    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h1) : "f"(r1 * mult));
+    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h2) : "f"(r2 * mult));
+    return b;
 }
 
 // One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
@@ -449,9 +457,10 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     const float k12 = kc.two_dt + kc.two_tau;
                     const int r = ty + 1, cc = tx + 4;
                     if constexpr (R16) {  // R^n = rho - a E^n
-                        r0 = fmaf(-kc.a, ea(0, r, cc), r16_decode(q0, w, 0));
-                        r1 = fmaf(-kc.a, ea(1, r, cc), r16_decode(q1, w, 1));
-                        r2 = fmaf(-kc.a, ea(2, r, cc), r16_decode(q2, w, 2));
+                        const float sc = r16_scale(w);
+                        r0 = fmaf(-kc.a, ea(0, r, cc), r16_decode(q0, sc));
+                        r1 = fmaf(-kc.a, ea(1, r, cc), r16_decode(q1, sc));
+                        r2 = fmaf(-kc.a, ea(2, r, cc), r16_decode(q2, sc));
                     }
                     if (ex_on) {
                         const float e = ea(0, r, cc);
@@ -484,19 +493,18 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             }
             if constexpr (R16) {
                 // every cell of the row segment is rewritten with the
-                // segment's new exponent (cells whose E is never updated
+                // segment's new scale (cells whose E is never updated
                 // store 0)
                 if (y < ny) {  // uniform over the warp: one warp is one row
-                    uint32_t b0, b1, b2;
-                    const unsigned short h0 = r16_encode(rho0, b0), h1 = r16_encode(rho1, b1),
-                                         h2 = r16_encode(rho2, b2);
+                    unsigned short h0, h1, h2;
+                    const uint32_t b = r16_encode(rho0, rho1, rho2, h0, h1, h2);
                     if (x < nx) {
                         reinterpret_cast<unsigned short *>(c.d_prev[0])[i] = h0;
                         reinterpret_cast<unsigned short *>(c.d_prev[1])[i] = h1;
                         reinterpret_cast<unsigned short *>(c.d_prev[2])[i] = h2;
                     }
                     if (tx == 0)
-                        c.r_exp[r16_word(c, z, bx, y)] = b0 | (b1 << 8) | (b2 << 16);
+                        c.r_exp[r16_word(c, z, bx, y)] = b;
                 }
             }
             } else {
@@ -869,7 +877,7 @@ bool fused_uses_tma(const NativeConsts &c)
 // Tensor maps of one step: E^n and H^{n-1/2} halo boxes (0-5), the tile
 // arrays (D form: D^n, D^{n-1}, E^{n-1} at 6-14; compact form: R at 6-8) and
 // the class volume after them; with 16-bit R (FP16 tiles at 6-8) the
-// exponent words at 10 (box: one segment's TY rows).
+// scale words at 10 (box: one segment's TY rows).
 bool encode_step_maps(const NativeConsts &c, bool compact, FusedMaps *maps, bool r16)
 {
     memset(maps, 0, sizeof *maps);
@@ -989,7 +997,7 @@ int launch_h_e_compact(const NativeConsts &c, cudaStream_t s)
 int launch_h_e_compact16(const NativeConsts &c, cudaStream_t s)
 {
     if (c.d_cur[0] != c.d_prev[0] || c.d_cur[1] != c.d_prev[1] || c.d_cur[2] != c.d_prev[2] || !c.r_exp)
-        return FDTD_ERR_INVALID;  // R and its exponent words are updated in place
+        return FDTD_ERR_INVALID;  // R and its scale words are updated in place
     FusedArgs a;
     a.c = c;
     a.zchunk = compact_zchunk(c.nz);

@@ -300,11 +300,11 @@ enum {
      * the reduced-storage form).  Stored per cell and component is the
      * residual rho = R^{n+1} + a E^{n+1} (a = 2 eps0 eps_inf tau), from
      * which the next step recovers R with the FP32 E it reads; rho is an
-     * FP16 value times a power of two shared by the 32 cells of one x-row
-     * segment of one plane (one exponent byte per component, placing the
-     * segment's largest residual just below 2^15, so every residual keeps
-     * FP16's 11 significant bits).  H and E stay FP32 and all arithmetic is
-     * FP32.  61.25
+     * FP16 value times a power of two shared by the three components of
+     * the 32 cells of one x-row segment of one plane (one scale per
+     * segment, placing its largest residual just below 2^15, so every
+     * residual keeps FP16's 11 significant bits).  H and E stay FP32 and all
+     * arithmetic is FP32.  61.25
      * instead of 73 bytes of traffic per cell update.  D is not stored, as
      * in FDTD_KERNEL_COMPACT. */
     FDTD_KERNEL_COMPACT_R16 = 3

@@ -1,7 +1,7 @@
 """Compact form with R stored in 16 bits (FDTD_KERNEL_COMPACT_R16): the
 compact form's update (updateEField, fdtd_calculations.cu:141-183, with D and
 E^{n-1} folded into R) with the residual R^{n+1} + a E^{n+1} held as an FP16
-value per cell and one power-of-two scale byte per component per 32-cell
+value per cell and one power-of-two scale per 32-cell
 row segment.  H, E and the arithmetic stay FP32, so the form is judged
 against the FP64 oracle at the reduced-storage tolerance R16_TOL (relative L2
 of each field and of each probe's E series), and against the 32-bit compact
@@ -117,7 +117,7 @@ def test_compact16_has_no_d_fields_and_zero_steps_stay_zero(cuda, tmp_path):
 
 @pytest.mark.parametrize("at", [0, 13])
 def test_compact16_checkpoint_resume_is_bit_identical(cuda, tmp_path, at):
-    """The checkpoint holds the FP16 residuals and their exponent words as stored."""
+    """The checkpoint holds the FP16 residuals and their scale words as stored."""
     p, codes, specs, a = _sphere(tmp_path / "a", 32, 60, fg.KERNEL_COMPACT_R16)
     a.run(at)
     a.checkpoint(tmp_path / "ck.bin")
