@@ -697,9 +697,9 @@ __global__ void __launch_bounds__(FTX *TY) fused_step_kernel(const __grid_consta
 // Many solves: persistent CTAs take work units from a counter; a unit's solve
 // descriptor supplies the constants (copied to shared memory) and tensor maps
 // (read by TMA from device memory).  Units of finished solves are skipped.
-// The compact form is bounded for 4 resident CTAs per SM (the 64-solve
+// The compact forms are bounded for 4 resident CTAs per SM (the 64-solve
 // workload ran 4.8 % faster than with 5: fewer units in flight, more
-// registers per thread).
+// registers per thread; with 16-bit R 11 % faster than with 3 or 5).
 template <int TY, int S, bool COMPACT, bool R16 = false>
 __global__ void __launch_bounds__(FTX *TY, COMPACT ? 4 : 3) batch_step_kernel(const BatchDesc *__restrict__ descs, int nsolves,
                                                              int total_units, int *work_counter)
