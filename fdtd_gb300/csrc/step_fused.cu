@@ -159,8 +159,8 @@ __device__ __forceinline__ size_t r16_word(const NativeConsts &c, int z, int bx,
 __device__ __forceinline__ float r16_scale(uint32_t w) { return __uint_as_float(w << 23); }
 
 // The residual of a cell from its stored FP16 bits h and its segment's
-// scale (exact: an FP16 value has 11 significant bits and the scale is a
-// normal power of two).
+// scale (exact while the product stays in FP32's normal range: an FP16
+// value has 11 significant bits and the scale is a power of two).
 __device__ __forceinline__ float r16_decode(unsigned short h, float scale)
 {
     float f;
