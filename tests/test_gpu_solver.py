@@ -195,3 +195,24 @@ def test_drop_in_voxel_cache_and_compact_binary_output(cuda, tmp_path):
     ez = s.field("ez")
     s.close()
     assert np.array_equal(runs[1].view(np.uint32), ez.view(np.uint32))
+
+
+def test_drop_in_compact16_binary_output_equals_the_solver(cuda, tmp_path):
+    """The drop-in with --kernel compact16 writes H and E only (no D files)
+    and its Ez bits equal the 16-bit-R solver's."""
+    import subprocess
+
+    n = 16
+    path = ph.c1_inputs(tmp_path, n=n, t_max=6)
+    out = tmp_path / "out"
+    out.mkdir()
+    r = subprocess.run([str(fg.EXE_PATH), "--params", str(path), "--specs", str(tmp_path / "mat_specs"),
+                        "--kernel", "compact16", "--format", "binary"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert not list(out.glob("D_field_*")) and len(list(out.glob("E_field_z_*.f32"))) == 6
+    got = np.fromfile(out / f"E_field_z_00005_z00000_n{n:05d}.f32", dtype="<f4").reshape(n, n, n)
+    p, codes, specs, s = solver_from_files(tmp_path / "again", n, 6, fg.KERNEL_COMPACT_R16)
+    s.run(6)
+    ez = s.field("ez")
+    s.close()
+    assert np.array_equal(got.view(np.uint32), ez.view(np.uint32))
