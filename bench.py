@@ -3,16 +3,20 @@
 
 Workload: 8 nested, seeded ellipsoids of Debye tissue in vacuum (uint8 class
 volume), a 900 MHz three-cell Ez dipole 20 cells outside the outer shell,
-Mur faces, dx = 1 mm, reference scheme, FP32 fields.  One step is one full
-Yee step (H, D + sources, Debye E, Mur) over all 104,857,600 cells.  The
-state (7.6 GB) is far larger than L2, so no flush is needed between steps.
+Mur faces, dx = 1 mm, dt = 0.99 of the Courant limit, corrected scheme (the
+reference scheme doubles |E| every step in vacuum; both schemes run the same
+kernels at the same speed), FP32 fields.  One step is one full Yee step (H,
+D + sources, Debye E, Mur) over all 104,857,600 cells.  The state (7.6 GB)
+is far larger than L2, so no flush is needed between steps.
 
 Default arm (``--impl gb300``): the library's solver, steps replayed as CUDA
 graphs; per-kernel times from fdtd_solver_profile give the roofline;
 ``e2e`` repeats the run through the C ABI with host buffers (material upload,
 a per-step Ez plane snapshot, final field read-back) inside the timed region.
 ``--impl reference`` times the CPU implementation of the reference kernels
-(the FP32 oracle port, bit-identical to them) on all host cores.
+(the FP32 oracle port, bit-identical to them) on all host threads, on the
+full grid, with inputs built by the oracle's own readers (no code of this
+library runs on that arm).
 
 Multi-GPU (torchrun): every rank runs its own solve (replicas, weak scaling);
 value = all ranks' cell-updates / slowest rank's time.
@@ -72,7 +76,8 @@ def parse_args():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--dims", type=int, nargs=3, default=[512, 512, 400], metavar=("NX", "NY", "NZ"))
     ap.add_argument("--kernel", choices=sorted(KERNELS), default="single")
-    ap.add_argument("--scheme", choices=["reference", "corrected"], default="reference")
+    ap.add_argument("--scheme", choices=["reference", "corrected"], default="corrected")
+    ap.add_argument("--timeskip", type=float, default=0.99, help="dt as a fraction of the Courant limit")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the compact-form line of the default run")
@@ -91,6 +96,8 @@ def parse_args():
     ap.add_argument("--serve-max-cells", type=float, default=0.0,
                     help="cap on the cells of the admitted solves (serve; 0: memory budget only)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
+    ap.add_argument("--ref-seconds", type=float, default=150.0,
+                    help="--impl reference: most seconds of timed CPU steps (fewer steps than --steps if needed)")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the probe/DFT/SAR error of the 16-bit-R form against the D form")
     ap.add_argument("--precision-steps", type=int, default=3000, help="steps of the precision comparison")
@@ -99,19 +106,55 @@ def parse_args():
 
 # ---------------------------------------------------------------- workload
 
-def make_workload(nx: int, ny: int, nz: int, tmp: Path):
-    """Phantom codes, class table and Params read back from input_params."""
-    import fdtd_gb300 as fg
-    from fdtd_gb300 import phantom as ph
+def _phantom_module():
+    """The input-file writer and phantom generator (pure numpy), loaded on its
+    own so that the reference arm runs no code of this library's package."""
+    import importlib.util
 
+    name = "fdtd_phantom_inputs"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, ROOT / "fdtd_gb300" / "phantom.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def write_workload_files(nx: int, ny: int, nz: int, tmp: Path):
+    """The phantom's class volume plus its input_params and mat_specs files
+    (the reference's formats) under tmp.  Returns (codes, number of classes)."""
+    ph = _phantom_module()
     codes, mats, cfg = ph.c2_config((nz, ny, nx))
     cfg.env_dir = str(tmp / "pgm")
     cfg.output_dir = str(tmp / "out")
     ph.write_input_params(tmp / "input_params", cfg)
     ph.write_mat_specs(tmp / "mat_specs", mats)
+    return codes, len(mats)
+
+
+def make_workload(nx: int, ny: int, nz: int, tmp: Path, timeskip: float):
+    """Phantom codes, class table and Params read back from input_params by
+    this library (the GPU arm)."""
+    import fdtd_gb300 as fg
+
+    codes, nmats = write_workload_files(nx, ny, nz, tmp)
     p = fg.Params.read(tmp / "input_params")
-    specs = fg.read_specs(tmp / "mat_specs")[: len(mats)]
+    p.set_timeskip(timeskip)
+    specs = fg.read_specs(tmp / "mat_specs")[:nmats]
     return p, codes, specs
+
+
+def oracle_inputs(tmp: Path, nmats: int, timeskip: float):
+    """The same workload files read by the oracle's restatement of the
+    reference's readers: params (initParamsWithPath + timeskip), mat_specs
+    records (loadMaterials) and the jz table (setupSources)."""
+    from oracle import pyoracle as po
+
+    q = po.params_read(tmp / "input_params", "f32")
+    po.set_timeskip(q, timeskip, "f32")
+    specs = po.read_specs(tmp / "mat_specs", "f32")[:nmats]
+    jz = po.setup_sources(q, "f32")
+    return q, specs, jz
 
 
 def workload_config(args, p) -> dict:
@@ -119,7 +162,7 @@ def workload_config(args, p) -> dict:
     return {"workload": f"nested-ellipsoid Debye phantom {nx}x{ny}x{nz}, 8 tissue classes + vacuum, "
                         f"900 MHz 3-cell Ez dipole, Mur ABC, dx=1 mm",
             "nx": nx, "ny": ny, "nz": nz, "cells": nx * ny * nz, "scheme": args.scheme, "kernel": args.kernel,
-            "sources": [list(s) for s in p.sources], "dt_s": float(p.dt),
+            "sources": [list(s) for s in p.sources], "dt_s": float(p.dt), "timeskip": args.timeskip,
             "l2": f"state {STATE_BYTES[args.kernel] * nx * ny * nz / 1e9:.1f} GB >> 129 MB L2: inputs larger "
                   f"than L2, no flush",
             "b_alg_bytes_per_cell_update": FORM_BYTES[args.kernel]}
@@ -202,54 +245,62 @@ def committed_traffic(kernel: str, cells: int):
 
 # ------------------------------------------------------------- CPU arms
 
-def cpu_port_rate(p, codes, specs, seconds: float, nthreads: int, max_steps: int | None = None):
-    """Cell-updates/s of the FP32 oracle port (bit-identical to the reference
-    kernels run on a CPU) on a z-slab of the workload."""
+def cpu_port_rate(q, codes, specs, jz, corrected: bool, warmup: int, max_steps: int, seconds: float) -> dict:
+    """The FP32 oracle port (bit-identical to the reference kernels run on a
+    CPU) on the full grid, OpenMP over (z, y) rows on every host thread the
+    process may use: ``warmup`` untimed steps, then timed steps until
+    ``max_steps`` or ``seconds`` is reached (at least one).  Returns the rate,
+    the threads that ran, the steps timed and the sample's description."""
     from oracle import pyoracle as po
 
-    nx, ny = p.nx, p.ny
-    sz = 8
-    srcz = p.sources[0][2] if p.sources else p.nz // 2
-    z0 = max(0, min(p.nz - sz, srcz - sz // 2))
-    slab = np.ascontiguousarray(codes[z0:z0 + sz])
-    media = po.Media(*(np.ascontiguousarray(specs[slab, k]) for k in (0, 2, 1, 3)))
-    media.rp = [np.ones(s, np.float32) for s in po.rp_shapes(nx, ny, sz)]
-    jz = p.setup_sources()
-    srcs = [(x, y, z - z0) for (x, y, z) in p.sources if z0 <= z < z0 + sz]
-    consts = dict(dt=p.dt, dx=p.dx, dy=p.dy, dz=p.dz, mu0=p.mu0, eps0=p.eps0)
-    cfg = po.make_cfg((nx, ny, sz), jz, sources=srcs, consts=consts, nthreads=nthreads)
-    st = po.State(nx, ny, sz, np.float32)
-    po.run(cfg, media, st, 0, 1)  # warm-up
+    nx, ny, nz = q.nx, q.ny, q.nz
+    media = po.Media(*(np.ascontiguousarray(specs[codes, k]) for k in (0, 2, 1, 3)))
+    default = [np.full((nz, ny, nx), v, np.float32)
+               for v in (q.default_sigma, q.default_eps_s, q.default_eps_i, q.default_tau_d)]
+    media.rp = po.setup_mur(q, *default)   # from the default material, as the reference does (fdtd.cu:59,65)
+    del default
+    cfg = po.make_cfg(q, jz, corrected=corrected)
+    threads = po.threads(cfg, "f32")
+    st = po.State(nx, ny, nz, np.float32)
+    po.run(cfg, media, st, 0, max(1, warmup))
     done, t0 = 0, time.perf_counter()
     while True:
-        po.run(cfg, media, st, 1 + done, 1)
+        po.run(cfg, media, st, max(1, warmup) + done, 1)
         done += 1
         el = time.perf_counter() - t0
-        if el >= seconds or (max_steps is not None and done >= max_steps):
+        if done >= max_steps or el >= seconds:
             break
-    cells = nx * ny * sz
-    return cells * done / el, f"{nx}x{ny}x{sz} z-slab of the workload, {done} steps, FP32 port of the reference kernels"
+    cells = nx * ny * nz
+    return {"rate": cells * done / el, "threads": threads, "steps": done, "ms_per_step": el / done * 1e3,
+            "sample": f"full {nx}x{ny}x{nz} grid, {max(1, warmup)} untimed + {done} timed steps, FP32 port of the "
+                      f"reference kernels (bit-identical to them), OpenMP over (z, y) rows on {threads} threads"}
 
 
 # ------------------------------------------------------------------- arms
 
 def run_reference_arm(args, rank: int, world: int) -> None:
+    """The reference's kernels on the host cores: the FP32 oracle port over
+    inputs read by the oracle's restatement of the reference's readers (no
+    code of this library's package runs here)."""
     if rank != 0:
         return
+    nx, ny, nz = args.dims
     with tempfile.TemporaryDirectory() as tmp:
-        nx, ny, nz = args.dims
-        p, codes, specs = make_workload(nx, ny, nz, Path(tmp))
-        threads = os.cpu_count() or 1
-        budget = max(10.0, min(120.0, args.cpu_seconds * 4))
-        rate, sample = cpu_port_rate(p, codes, specs, budget, threads, max_steps=args.steps)
-        cfg = workload_config(args, p)
-    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": nx * ny * nz / rate * 1e3,
+        codes, nmats = write_workload_files(nx, ny, nz, Path(tmp))
+        q, specs, jz = oracle_inputs(Path(tmp), nmats, args.timeskip)
+    r = cpu_port_rate(q, codes, specs, jz, args.scheme == "corrected", args.warmup, args.steps, args.ref_seconds)
+    cfg = {"workload": f"nested-ellipsoid Debye phantom {nx}x{ny}x{nz}, 8 tissue classes + vacuum, "
+                       f"900 MHz 3-cell Ez dipole, Mur ABC, dx=1 mm",
+           "nx": nx, "ny": ny, "nz": nz, "cells": nx * ny * nz, "scheme": args.scheme, "kernel": "reference",
+           "sources": [list(t) for t in q.source_list()], "dt_s": float(q.dt), "timeskip": args.timeskip,
+           "b_alg_bytes_per_cell_update": B_ALG}
+    line = {"impl": "reference", "metric": METRIC, "value": r["rate"], "unit": "cell-updates/s", "n_gpus": args.gpus,
+            "steps": r["steps"], "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": cfg,
-            "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-                             "sample": sample},
-            "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "cpu_baseline": {"value": r["rate"], "unit": "cell-updates/s", "cores": r["threads"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": r["rate"], "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
@@ -266,20 +317,40 @@ def precision_probes(codes: np.ndarray, n: int = PRECISION_PROBES, seed: int = P
     return [(int(a), int(b), int(c)) for a, b, c in zip(x, y, z)]
 
 
-def precision_check(p, codes, specs, dev: int, steps: int) -> dict:
-    """Error of the 16-bit-R compact form (and of the 32-bit compact form)
-    against the D form, all on the GPU, corrected scheme, `steps` steps:
-    E series at 16 seeded probe points inside the phantom (relative L2 per
-    probe over the 3 components and all steps), the running DFT |E| at the
-    source's 900 MHz over 32 planes through the source, and the peak
-    spectral SAR over those planes.  The D form itself is held to the FP64
-    oracle by the parity tests (grids the oracle runs in seconds)."""
+C3_FIXTURE = ROOT / "tests" / "golden" / "c3_fp64.npz"
+
+
+def c3_fixture(p, codes, specs, steps: int, scheme: str):
+    """The FP64 oracle's record of this workload (tests/golden/c3_fp64.npz),
+    when it describes exactly these inputs, else None."""
+    import hashlib
+
+    if not C3_FIXTURE.exists() or scheme != "corrected":
+        return None
+    f = np.load(C3_FIXTURE)
+    same = (tuple(int(v) for v in f["shape"]) == codes.shape and int(f["steps"]) == steps
+            and np.float32(p.dt) == f["dt"] and np.array_equal(f["specs"], specs)
+            and str(f["codes_sha256"]) == hashlib.sha256(codes.tobytes()).hexdigest())
+    return f if same else None
+
+
+def precision_check(p, codes, specs, dev: int, steps: int, scheme: str) -> dict:
+    """Error of the 16-bit-R compact form, the 32-bit compact form and the D
+    form against the FP64 oracle, corrected scheme, `steps` steps: E series at
+    16 seeded probe points inside the phantom (relative L2 per probe over the
+    3 components and all steps), the running DFT |E| at the source's 900 MHz
+    over 32 planes through the source (on every 4th cell in x and y, as the
+    oracle's record holds it), and the peak spectral SAR over those planes.
+    The FP64 record comes from tests/golden/make_c3_fixture.py; without one for
+    this workload the D form on the GPU stands in for it."""
     import fdtd_gb300 as fg
 
     nz = codes.shape[0]
-    probes = precision_probes(codes)
+    fx = c3_fixture(p, codes, specs, steps, scheme)
+    probes = [tuple(int(v) for v in r) for r in fx["probes"]] if fx is not None else precision_probes(codes)
     freq = float(p.waveFrequency) * float(p.pulseModulationFrequency)
     z0, nplanes = max(0, nz // 2 - 16), min(32, nz)
+    sub = int(fx["dft_sub"]) if fx is not None else 1
 
     def run(kernel):
         s = fg.Solver(p, codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel, device=dev)
@@ -294,19 +365,57 @@ def precision_check(p, codes, specs, dev: int, steps: int) -> dict:
             e2 = np.abs(a) ** 2 if e2 is None else e2 + np.abs(a) ** 2
         sar, cell = s.peak_sar()
         s.close()
-        return series, np.sqrt(e2), sar, cell
+        return series, np.sqrt(e2)[:, ::sub, ::sub], sar, cell
 
-    ref = run(fg.KERNEL_SINGLE_PASS)
-    out = {"reference": "FP32 D form on the GPU (same workload, corrected scheme)", "steps": steps,
-           "probes": probes, "dft_hz": freq, "dft_planes": [z0, z0 + nplanes]}
-    for name, kernel in (("compact16", fg.KERNEL_COMPACT_R16), ("compact", fg.KERNEL_COMPACT)):
+    if fx is not None:
+        pc = fx["peak_sar_cell"]
+        ny, nx = codes.shape[1:]
+        ref = (fx["series"].astype(np.float64), fx["dft_abs_e_sub"].astype(np.float64), float(fx["peak_sar"]),
+               int((pc[2] * ny + pc[1]) * nx + pc[0]))
+        what = ("FP64 CPU oracle (tests/golden/c3_fp64.npz: same phantom, corrected scheme, dt 0.99 of the "
+                "Courant limit)")
+        forms = (("compact16", fg.KERNEL_COMPACT_R16), ("compact", fg.KERNEL_COMPACT), ("d_form", fg.KERNEL_SINGLE_PASS))
+    else:
+        ref = run(fg.KERNEL_SINGLE_PASS)
+        what = "FP32 D form on the GPU (no FP64 record of this workload)"
+        forms = (("compact16", fg.KERNEL_COMPACT_R16), ("compact", fg.KERNEL_COMPACT))
+    out = {"reference": what, "steps": steps, "probes": probes, "dft_hz": freq, "dft_planes": [z0, z0 + nplanes],
+           "dft_cells": f"every {sub}th cell in x and y" if sub > 1 else "all"}
+    for name, kernel in forms:
         series, amp, sar, cell = run(kernel)
         per = [float(np.linalg.norm(series[:, j] - ref[0][:, j]) / max(np.linalg.norm(ref[0][:, j]), 1e-300))
                for j in range(len(probes))]
         out[name] = {"probe_rel_l2_max": max(per), "probe_rel_l2_median": float(np.median(per)),
+                     "probe_rel_l2": per,
                      "dft_abs_e_rel_l2": float(np.linalg.norm(amp - ref[1]) / np.linalg.norm(ref[1])),
                      "peak_sar_rel": float(abs(sar - ref[2]) / ref[2]), "peak_sar_same_cell": cell == ref[3]}
     return out
+
+
+def ref_cuda_leg(q, codes, specs, jz, dev: int, steps: int = 300, warmup: int = 6) -> dict | None:
+    """The reference's own CUDA kernels (fdtd_calculations.cu compiled for
+    sm_103a with its Makefile's nvcc defaults, run from the cubin with its
+    launch grid and slot rotation, output gated) on this workload and GPU,
+    outside the timed region.  Steps stay below 512 (the reference's dJz
+    table); None where the cubin was not built."""
+    from oracle import pyoracle as po
+
+    if not po.ref_gpu_available():
+        return None
+    nx, ny, nz = q.nx, q.ny, q.nz
+    media = po.Media(*(np.ascontiguousarray(specs[codes, k]) for k in (0, 2, 1, 3)))
+    default = [np.full((nz, ny, nx), v, np.float32)
+               for v in (q.default_sigma, q.default_eps_s, q.default_eps_i, q.default_tau_d)]
+    media.rp = po.setup_mur(q, *default)
+    del default
+    with ClockSampler(dev) as clk:
+        ms = po.ref_gpu_run(po.make_cfg(q, jz), media, steps, warmup=warmup)
+    cells = nx * ny * nz
+    return {"value": cells * steps / (ms / 1e3), "unit": "cell-updates/s", "ms_per_step": ms / steps,
+            "steps": steps, "warmup": warmup, "clocks": clk.summary(),
+            "what": "the reference's fdtd_calculations.cu kernels (nvcc defaults, sm_103a) with its launch grid "
+                    "(ceil(nx/128) x ny x nz blocks of 128) and slot rotation, reference scheme, same workload, "
+                    "same GPU, CUDA events around the steps"}
 
 
 def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
@@ -321,7 +430,7 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
     kernel = KERNELS[args.kernel]
     scheme = fg.SCHEME_REFERENCE if args.scheme == "reference" else fg.SCHEME_CORRECTED
     tmp = tempfile.TemporaryDirectory()
-    p, codes, specs = make_workload(nx, ny, nz, Path(tmp.name))
+    p, codes, specs = make_workload(nx, ny, nz, Path(tmp.name), args.timeskip)
 
     # ---- device-resident throughput (value)
     s = fg.Solver(p, codes, specs, scheme=scheme, kernel=kernel, device=local_rank)
@@ -377,7 +486,8 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
                 "roofline_traffic": committed_traffic(cmain, cells),
                 "gpu_launches": len(cprof) * args.steps, "clocks": cclk.summary()}
         if not args.no_precision:
-            forms["compact16"]["precision"] = precision_check(p, codes, specs, local_rank, args.precision_steps)
+            forms["compact16"]["precision"] = precision_check(p, codes, specs, local_rank, args.precision_steps,
+                                                              args.scheme)
 
     # ---- end to end through the C ABI with host buffers (e2e)
     e2e = None
@@ -405,12 +515,17 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
                "includes": "solver create (material + plan upload), per-step Ez plane D2H through the pinned "
                            "snapshot ring, final Ez volume read-back, destroy"}
 
-    # ---- CPU baseline (rank 0, N = 1 only)
-    cpu = None
+    # ---- CPU baseline and the reference's CUDA kernels (rank 0, N = 1 only;
+    # inputs read by the oracle's restatement of the reference's readers)
+    cpu = ref_cuda = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
-        rate, sample = cpu_port_rate(p, codes, specs, args.cpu_seconds, threads)
-        cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port", "sample": sample}
+        q, ospecs, jz = oracle_inputs(Path(tmp.name), len(specs), args.timeskip)
+        r = cpu_port_rate(q, codes, ospecs, jz, args.scheme == "corrected", 2, 10 ** 6, args.cpu_seconds)
+        cpu = {"value": r["rate"], "unit": "cell-updates/s", "cores": r["threads"], "kind": "port",
+               "sample": r["sample"]}
+        ref_cuda = ref_cuda_leg(q, codes, ospecs, jz, local_rank)
+        if ref_cuda is not None:
+            ref_cuda["speedup_value_vs_ref_cuda"] = (total_cells / tmax) / ref_cuda["value"]
     tmp.cleanup()
 
     if rank != 0:
@@ -436,6 +551,7 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
         "clocks": clocks,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "ref_cuda_baseline": ref_cuda,
     }
     if forms:
         for f in forms.values():
@@ -576,6 +692,11 @@ def main() -> None:
         torch.cuda.set_device(0)
         (run_batch_workload if args.workload == "batch" else run_serve_workload)(args)
         return
+    if args.impl == "reference":
+        # rank 0 alone runs the CPU arm; other ranks exit without work (no
+        # process group: the arm has no exchange)
+        run_reference_arm(args, int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)))
+        return
     from fdtd_gb300 import replicas
 
     rank, local_rank, world = replicas.dist_env()
@@ -584,15 +705,11 @@ def main() -> None:
         import torch
         import torch.distributed as td
 
-        if args.impl == "gb300":
-            torch.cuda.set_device(local_rank)
-        td.init_process_group("nccl" if args.impl == "gb300" else "gloo")
+        torch.cuda.set_device(local_rank)
+        td.init_process_group("nccl")
         dist = td
     try:
-        if args.impl == "reference":
-            run_reference_arm(args, rank, world)
-        else:
-            run_gb300_arm(args, rank, local_rank, world, dist)
+        run_gb300_arm(args, rank, local_rank, world, dist)
     finally:
         if dist is not None:
             dist.destroy_process_group()

@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["compat.cu", "native.cu", "step_fused.cu", "step_static.cu", "solver.cu", "monitor.cu", "batch.cu", "cuda_util.cu"]
 CPP_SOURCES = ["host_io.cpp"]
-HEADERS = ["fdtd_internal.h", "device_common.cuh", "native.cuh", "solver_internal.cuh", "tma_util.cuh"]
+HEADERS = ["fdtd_internal.h", "device_common.cuh", "native.cuh", "solver_internal.cuh", "tma_util.cuh", "per_device.h"]
 
 
 def _run(cmd: list[str]) -> str:

@@ -26,9 +26,8 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
-#include <mutex>
-
 #include "native.cuh"
+#include "per_device.h"
 #include "tma_util.cuh"
 
 namespace fdtd {
@@ -817,13 +816,20 @@ int launch_fused_impl(const FusedArgs &a, const FusedMaps &maps, cudaStream_t s)
 {
     auto kernel = fused_step_kernel<TY_SEL, S_SEL, TMA, COMPACT, R16>;
     using G = GeoOf<TY_SEL, COMPACT, R16>;
-    static std::once_flag once;
-    std::call_once(once, [&] {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             fused_smem_bytes<S_SEL, G>(FDTD_MAX_CLASSES));
-    });
     if (a.c.nclasses < 1 || a.c.nclasses > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
+    // the shared-memory opt-in holds for the current device only
+    static PerDeviceOnce<> smem_opt_in;
+    int dev = 0;
+    cudaError_t de = cudaGetDevice(&dev);
+    if (de != cudaSuccess)
+        return (int)de;
+    const int so = smem_opt_in.run(dev, [&] {
+        return (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         fused_smem_bytes<S_SEL, G>(FDTD_MAX_CLASSES));
+    });
+    if (so != 0)
+        return so < 0 ? FDTD_ERR_INVALID : so;
     const int smem = fused_smem_bytes<S_SEL, G>(a.c.nclasses);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((a.c.nx + FTX - 1) / FTX, (a.c.ny + TY_SEL - 1) / TY_SEL, (a.c.nz + a.zchunk - 1) / a.zchunk);
@@ -918,15 +924,29 @@ int fused_tile_height() { return TY_SEL; }
 template <bool COMPACT, bool R16 = false>
 int batch_smem(int nclasses) { return fused_smem_bytes<S_SEL, GeoOf<TY_SEL, COMPACT, R16>>(nclasses); }
 
+// The batch kernel's shared-memory opt-in on the current device (it holds
+// for that device only): made on the first use there.
+template <bool COMPACT, bool R16 = false>
+int batch_opt_in()
+{
+    auto kernel = batch_step_kernel<TY_SEL, S_SEL, COMPACT, R16>;
+    static PerDeviceOnce<> smem_opt_in;
+    int dev = 0;
+    const cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return (int)e;
+    const int so = smem_opt_in.run(dev, [&] {
+        return (int)cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         batch_smem<COMPACT, R16>(FDTD_MAX_CLASSES));
+    });
+    return so < 0 ? FDTD_ERR_INVALID : so;
+}
+
 template <bool COMPACT, bool R16 = false>
 int batch_ctas_impl(int nclasses)
 {
     auto kernel = batch_step_kernel<TY_SEL, S_SEL, COMPACT, R16>;
-    static std::once_flag once;
-    std::call_once(once, [&] {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             batch_smem<COMPACT, R16>(FDTD_MAX_CLASSES));
-    });
+    batch_opt_in<COMPACT, R16>();
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -945,6 +965,9 @@ int launch_batch_step(const BatchLaunch &b, cudaStream_t s)
 {
     if (b.max_classes < 1 || b.max_classes > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
+    const int oi = b.r16 ? batch_opt_in<true, true>() : (b.compact ? batch_opt_in<true>() : batch_opt_in<false>());
+    if (oi != FDTD_OK)
+        return oi;
     if (b.r16)
         batch_step_kernel<TY_SEL, S_SEL, true, true>
             <<<b.persistent_ctas, dim3(FTX, TY_SEL), batch_smem<true, true>(b.max_classes), s>>>(

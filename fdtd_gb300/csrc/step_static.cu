@@ -17,6 +17,7 @@
 // array until the process exits.  All calls share it and it keeps the last
 // call's contents: each call rewrites the class table and the source sample
 // and clears the error word, so calls whose work overlaps on the GPU race.
+#include <algorithm>
 #include <mutex>
 
 #include "native.cuh"
@@ -72,6 +73,10 @@ extern "C" int fdtd_step_static(const FdtdParams *p, const float *specs, int ncl
         return FDTD_ERR_INVALID;  // the class table must fit the static array
     if (p->sourcesCount < 0 || p->sourcesCount > FDTD_MAX_SOURCES || (p->sourcesCount > 0 && !p->sources))
         return FDTD_ERR_INVALID;
+    // the source sample comes from the caller's jz table (this call builds no
+    // table): with sources, a table must be given
+    if (p->sourcesCount > 0 && (!p->jz || p->jzCount < 1))
+        return FDTD_ERR_INVALID;
     for (int s = 0; s < p->sourcesCount; s++) {
         const int *q = p->sources + 3 * s;
         if (q[0] < 1 || q[0] >= p->nx || q[1] < 1 || q[1] >= p->ny || q[2] < 0 || q[2] >= p->nz)
@@ -102,8 +107,11 @@ extern "C" int fdtd_step_static(const FdtdParams *p, const float *specs, int ncl
     DebyeCoef coef[FDTD_STATIC_MAX_CLASSES];
     for (int k = 0; k < nclasses; k++)
         coef[k] = debye_coef(p->dt, p->eps0, specs[4 * k], specs[4 * k + 1], specs[4 * k + 2], specs[4 * k + 3], scheme);
+    // the sample of step n, from the first FDTD_JZ_LEN entries of the table
+    // as fdtd_plan_create keeps them (beyond them the sample is 0)
     const int j = scheme == FDTD_SCHEME_CORRECTED ? n : n - n % 3;
-    const float jz = (p->jz && j < p->jzCount) ? p->jz[j] : 0.0f;
+    const int njz = p->jz ? std::min(p->jzCount, FDTD_JZ_LEN) : 0;
+    const float jz = j < njz ? p->jz[j] : 0.0f;
     struct {
         float jz;
         int err;
@@ -155,12 +163,12 @@ extern "C" int fdtd_step_static(const FdtdParams *p, const float *specs, int ncl
         st = launch_mur(c, stream);
     if (st != FDTD_OK)
         return st;
-    // wait for the step and report a bounded wait that gave up
-    e = cudaStreamSynchronize(stream);
-    if (e != cudaSuccess)
-        return e;
+    // read the error word behind the step on the caller's stream, wait for
+    // both, and report a bounded wait that gave up
     int err = 0;
-    e = cudaMemcpy(&err, d_err, sizeof err, cudaMemcpyDeviceToHost);
+    e = cudaMemcpyAsync(&err, d_err, sizeof err, cudaMemcpyDeviceToHost, stream);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(stream);
     if (e != cudaSuccess)
         return e;
     return err ? FDTD_ERR_DEVICE_TIMEOUT : FDTD_OK;

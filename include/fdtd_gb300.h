@@ -263,7 +263,10 @@ int fdtd_step(const fdtd_plan *plan, const fdtd_native_fields *f, int n, fdtd_st
  * step's source sample and an error word in a file-scope __device__ array of
  * FDTD_STATIC_SCRATCH_BYTES bytes, which every GPU that loads the library
  * holds until the process exits; everything else comes from the caller:
- * p (grid, dt, dx.., sources, host jz table), specs (host, nclasses x 4,
+ * p (grid, dt, dx.., sources, host jz table: required when there are
+ * sources, else FDTD_ERR_INVALID; the sample of step n is jz[n] (corrected
+ * scheme) or jz[n - n%3] (reference scheme) when that index is below
+ * min(jzCount, FDTD_JZ_LEN), else 0, as in the plan), specs (host, nclasses x 4,
  * nclasses <= FDTD_STATIC_MAX_CLASSES, else FDTD_ERR_INVALID), the device
  * fields f (hx_out..hz_out must not alias hx..hz), the six device Mur slabs
  * rp_dev (rpx0, rpy0, rpz0, rpxEnd, rpyEnd, rpzEnd) and the step index n.

@@ -14,9 +14,12 @@
   drives the reference kernels on the GPU (``ref/ref_gpu.cu``); built on every
   host with nvcc, used only where the cubin exists.
 
-The ``_ref`` libraries are built only where the reference sources exist
-(``FDTD_REFERENCE_ROOT``, default ``/root/reference``); they compile the
-reference files where they lie and write nothing but ``oracle/_ref/``.
+The ``_ref`` libraries are built only where the reference sources exist: the
+directory ``FDTD_REFERENCE_ROOT`` names, else the build container's mount of
+the reference (this recipe is the one file that reads the sources where they
+lie).  They compile the reference files in place and write nothing but
+``oracle/_ref/``; the GPU machine, which has no reference sources, uses the
+files built here.
 Both builds use ``-ffp-contract=off`` so x86 and Arm hosts give identical bits.
 """
 from __future__ import annotations

@@ -112,7 +112,8 @@ static void set_threads(const oracle_cfg *cfg)
 }
 
 /* H <- H - dt/mu0 curl E, in place (fdtd_calculations.cu:32-77).  The hx
- * z-derivative is scaled by dy, as in the reference (:51). */
+ * z-derivative is scaled by dy, as in the reference (:51).  Work is shared
+ * over (z, y) rows so that every host thread has rows even on thin slabs. */
 static void update_h(const oracle_cfg *cfg, real *hx, real *hy, real *hz,
                      const real *ex, const real *ey, const real *ez)
 {
@@ -121,21 +122,22 @@ static void update_h(const oracle_cfg *cfg, real *hx, real *hy, real *hz,
     const real kx = dt / (mu0 * (real)cfg->dx);
     const real ky = dt / (mu0 * (real)cfg->dy);
     const real kz = dt / (mu0 * (real)cfg->dz);
-    #pragma omp parallel for schedule(static)
+    /* hx: y in [0,ny-2]; hy: y in [1,ny-2]; hz: y in [0,ny-2], z >= 1 */
+    #pragma omp parallel for collapse(2) schedule(static)
     for (int z = 0; z < nz - 1; z++) {
-        for (int y = 0; y < ny - 1; y++)
+        for (int y = 0; y < ny - 1; y++) {
             for (int x = 1; x < nx - 1; x++)
                 AT(hx, x, y, z) = AT(hx, x, y, z) - ky * (AT(ez, x, y + 1, z) - AT(ez, x, y, z))
                                                   + ky * (AT(ey, x, y, z + 1) - AT(ey, x, y, z));
-        for (int y = 1; y < ny - 1; y++)
-            for (int x = 0; x < nx - 1; x++)
-                AT(hy, x, y, z) = AT(hy, x, y, z) - kz * (AT(ex, x, y, z + 1) - AT(ex, x, y, z))
-                                                  + kx * (AT(ez, x + 1, y, z) - AT(ez, x, y, z));
-        if (z >= 1)
-            for (int y = 0; y < ny - 1; y++)
+            if (y >= 1)
+                for (int x = 0; x < nx - 1; x++)
+                    AT(hy, x, y, z) = AT(hy, x, y, z) - kz * (AT(ex, x, y, z + 1) - AT(ex, x, y, z))
+                                                      + kx * (AT(ez, x + 1, y, z) - AT(ez, x, y, z));
+            if (z >= 1)
                 for (int x = 0; x < nx - 1; x++)
                     AT(hz, x, y, z) = AT(hz, x, y, z) - kx * (AT(ey, x + 1, y, z) - AT(ey, x, y, z))
                                                       + ky * (AT(ex, x, y + 1, z) - AT(ex, x, y, z));
+        }
     }
 }
 
@@ -150,22 +152,23 @@ static void update_d(const oracle_cfg *cfg, real *const dt_[3], real *const ds[3
     const real tz = (real)cfg->dt / (real)cfg->dz;
     real *dxT = dt_[0], *dyT = dt_[1], *dzT = dt_[2];
     const real *dxS = ds[0], *dyS = ds[1], *dzS = ds[2];
-    #pragma omp parallel for schedule(static)
+    /* dx: y, z in [1,n-2]; dy: y in [0,ny-2], z in [1,nz-2]; dz: y in [1,ny-2], z in [0,nz-2] */
+    #pragma omp parallel for collapse(2) schedule(static)
     for (int z = 0; z < nz - 1; z++) {
-        if (z >= 1) {
-            for (int y = 1; y < ny - 1; y++)
+        for (int y = 0; y < ny - 1; y++) {
+            if (z >= 1 && y >= 1)
                 for (int x = 0; x < nx - 1; x++)
                     AT(dxT, x, y, z) = AT(dxS, x, y, z) + ty * (AT(hz, x, y, z) - AT(hz, x, y - 1, z))
                                                         - tz * (AT(hy, x, y, z) - AT(hy, x, y, z - 1));
-            for (int y = 0; y < ny - 1; y++)
+            if (z >= 1)
                 for (int x = 1; x < nx - 1; x++)
                     AT(dyT, x, y, z) = AT(dyS, x, y, z) + tz * (AT(hx, x, y, z) - AT(hx, x, y, z - 1))
                                                         - tx * (AT(hz, x, y, z) - AT(hz, x - 1, y, z));
+            if (y >= 1)
+                for (int x = 1; x < nx - 1; x++)
+                    AT(dzT, x, y, z) = AT(dzS, x, y, z) + tx * (AT(hy, x, y, z) - AT(hy, x - 1, y, z))
+                                                        - ty * (AT(hx, x, y, z) - AT(hx, x, y - 1, z));
         }
-        for (int y = 1; y < ny - 1; y++)
-            for (int x = 1; x < nx - 1; x++)
-                AT(dzT, x, y, z) = AT(dzS, x, y, z) + tx * (AT(hy, x, y, z) - AT(hy, x - 1, y, z))
-                                                    - ty * (AT(hx, x, y, z) - AT(hx, x, y - 1, z));
     }
     /* updateSources: the device table holds jz[0..511]; larger indices are
      * undefined in the reference, here they read the host table. */
@@ -189,7 +192,7 @@ static void update_e(const oracle_cfg *cfg, const oracle_media *m,
     const int nx = cfg->nx, ny = cfg->ny, nz = cfg->nz;
     const real dt = cfg->dt, eps0 = cfg->eps0;
     const int corrected = cfg->corrected;
-    #pragma omp parallel for schedule(static)
+    #pragma omp parallel for collapse(2) schedule(static)
     for (int z = 0; z < nz; z++) {
         for (int y = 0; y < ny; y++) {
             for (int x = 0; x < nx; x++) {
@@ -230,7 +233,8 @@ static inline real mur_cell(real dt, real h, real mu0eps0, real rp_self, real rp
 
 /* updateMurBoundary (fdtd_calculations.cu:216-428): tangential E on the six
  * faces, edges excluded.  With every dimension >= 3 no face reads a cell that
- * another face writes, so the face order does not matter. */
+ * another face writes, so the face order does not matter, and the cells of
+ * one face loop are independent (each loop is shared over host threads). */
 static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
                        real *const eT[3], real *const eS[3])
 {
@@ -242,6 +246,7 @@ static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
     const int fix = cfg->corrected;
 
     /* ex on y faces (rpy) and z faces (rpz) */
+    #pragma omp parallel for schedule(static)
     for (int z = 1; z < nz - 1; z++)
         for (int x = 0; x < nx - 1; x++) {
             AT(exT, x, 0, z) = mur_cell(dt, hy_, me, RPY(m->rpy0, x, 0, z), RPY(m->rpy0, x, 1, z),
@@ -249,6 +254,7 @@ static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
             AT(exT, x, ny - 1, z) = mur_cell(dt, hy_, me, RPY(m->rpy_end, x, 1, z), RPY(m->rpy_end, x, 0, z),
                                              AT(exT, x, ny - 2, z), AT(exS, x, ny - 2, z), AT(exS, x, ny - 1, z));
         }
+    #pragma omp parallel for schedule(static)
     for (int y = 1; y < ny - 1; y++)
         for (int x = 0; x < nx - 1; x++) {
             AT(exT, x, y, 0) = mur_cell(dt, hz_, me, RPZ(m->rpz0, x, y, 0), RPZ(m->rpz0, x, y, 1),
@@ -258,6 +264,7 @@ static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
         }
     /* ey on x faces (rpx) and z faces (rpz).  At x = nx-1 the reference reads
      * E^n at x-1 in the first term as well (fdtd_calculations.cu:323). */
+    #pragma omp parallel for schedule(static)
     for (int z = 1; z < nz - 1; z++)
         for (int y = 0; y < ny - 1; y++) {
             AT(eyT, 0, y, z) = mur_cell(dt, hx_, me, RPX(m->rpx0, 0, y, z), RPX(m->rpx0, 1, y, z),
@@ -266,6 +273,7 @@ static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
             AT(eyT, nx - 1, y, z) = mur_cell(dt, hx_, me, RPX(m->rpx_end, 1, y, z), RPX(m->rpx_end, 0, y, z),
                                              first, AT(eyS, nx - 2, y, z), AT(eyS, nx - 1, y, z));
         }
+    #pragma omp parallel for schedule(static)
     for (int y = 0; y < ny - 1; y++)
         for (int x = 1; x < nx - 1; x++) {
             AT(eyT, x, y, 0) = mur_cell(dt, hz_, me, RPZ(m->rpz0, x, y, 0), RPZ(m->rpz0, x, y, 1),
@@ -274,6 +282,7 @@ static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
                                              AT(eyT, x, y, nz - 2), AT(eyS, x, y, nz - 2), AT(eyS, x, y, nz - 1));
         }
     /* ez on x faces (rpx) and y faces (rpy) */
+    #pragma omp parallel for schedule(static)
     for (int z = 0; z < nz - 1; z++)
         for (int y = 1; y < ny - 1; y++) {
             AT(ezT, 0, y, z) = mur_cell(dt, hx_, me, RPX(m->rpx0, 0, y, z), RPX(m->rpx0, 1, y, z),
@@ -281,6 +290,7 @@ static void update_mur(const oracle_cfg *cfg, const oracle_media *m,
             AT(ezT, nx - 1, y, z) = mur_cell(dt, hx_, me, RPX(m->rpx_end, 1, y, z), RPX(m->rpx_end, 0, y, z),
                                              AT(ezT, nx - 2, y, z), AT(ezS, nx - 2, y, z), AT(ezS, nx - 1, y, z));
         }
+    #pragma omp parallel for schedule(static)
     for (int z = 0; z < nz - 1; z++)
         for (int x = 1; x < nx - 1; x++) {
             AT(ezT, x, 0, z) = mur_cell(dt, hy_, me, RPY(m->rpy0, x, 0, z), RPY(m->rpy0, x, 1, z),
@@ -344,6 +354,19 @@ int oracle_update_mur(const oracle_cfg *cfg, const oracle_media *m, real *eT[3],
 
 int oracle_real_size(void) { return (int)sizeof(real); }
 
+/* Host threads the loops above run on for cfg (nthreads <= 0: the OpenMP
+ * default, i.e. every core the process may use). */
+int oracle_threads(const oracle_cfg *cfg)
+{
+#ifdef _OPENMP
+    set_threads(cfg);
+    return omp_get_max_threads();
+#else
+    (void)cfg;
+    return 1;
+#endif
+}
+
 /* ------------------------------------------------------------------ setup */
 
 /* initParamsWithPath (fdtd.cu:547-637): fixed line order, keys ignored. */
@@ -401,6 +424,19 @@ int oracle_params_read(const char *path, oracle_params *p)
             (p->c * sqrt(1.0 / pow(p->dx, 2.0) + 1.0 / pow(p->dy, 2.0) + 1.0 / pow(p->dz, 2.0)));
     p->mu0 = 4.0 * p->pi * pow(10.0, -7.0);
     p->eps0 = 1.0 / (p->mu0 * p->c * p->c);
+    return 0;
+}
+
+/* dt for a Courant factor other than the reference's fixed timeskip = 1.0
+ * (fdtd.cu:629-631 with timeskip as given; used for the 0.99 CFL step of the
+ * benchmark configurations). */
+int oracle_params_set_timeskip(oracle_params *p, float timeskip)
+{
+    if (!(timeskip > 0.0f) || p->elements_per_wave <= 0 || !(p->wave_frequency > 0.0f))
+        return -1;
+    p->timeskip = timeskip;
+    p->dt = 1.0 * p->timeskip /
+            (p->c * sqrt(1.0 / pow(p->dx, 2.0) + 1.0 / pow(p->dy, 2.0) + 1.0 / pow(p->dz, 2.0)));
     return 0;
 }
 
@@ -512,13 +548,13 @@ int oracle_setup_mur(const oracle_params *p, const float *sigma, const float *ep
     return 0;
 }
 
-/* loadMaterials (fdtd.cu:875-939).  At most 94 mat_specs records are read;
- * a record that fails to scan re-stores the previous one; reading stops after
- * a code >= 94.  specs receives 256 x 4 floats (sigma, eps_s, eps_i, tau).
- * Then nz slices <dir>/v1_%05d.pgm (1-based) are read: a 6-token header, then
+/* loadMaterials (fdtd.cu:875-939).  oracle_read_specs is its mat_specs part
+ * (:880-904): at most 94 records are read; a record that fails to scan
+ * re-stores the previous one; reading stops after a code >= 94.  specs
+ * receives 256 x 4 floats (sigma, eps_s, eps_i, tau).
+ * oracle_load_materials then reads nz slices <dir>/v1_%05d.pgm (1-based) are read: a 6-token header, then
  * nx*ny codes as one flat stream, x fastest.  codes may be NULL. */
-int oracle_load_materials(const oracle_params *p, const char *specs_path, const char *dir,
-                          float *specs, uint8_t *codes, float *sigma, float *eps_s, float *eps_i, float *tau)
+int oracle_read_specs(const char *specs_path, float *specs)
 {
     char tmp[1024];
     memset(specs, 0, sizeof(float) * 4 * ORACLE_SPEC_CODES);
@@ -541,6 +577,16 @@ int oracle_load_materials(const oracle_params *p, const char *specs_path, const 
             break;
     }
     fclose(f);
+    return 0;
+}
+
+int oracle_load_materials(const oracle_params *p, const char *specs_path, const char *dir,
+                          float *specs, uint8_t *codes, float *sigma, float *eps_s, float *eps_i, float *tau)
+{
+    char tmp[1024];
+    const int rs = oracle_read_specs(specs_path, specs);
+    if (rs != 0)
+        return rs;
     const size_t plane = (size_t)p->nx * p->ny;
     for (int z = 0; z < p->nz; z++) {
         char name[2100];

@@ -91,6 +91,27 @@ def params_read(path: str | Path, which: str = "f64") -> OracleParams:
     return p
 
 
+def set_timeskip(p: OracleParams, timeskip: float, which: str = "f64") -> None:
+    """dt for the Courant factor ``timeskip`` (the reference fixes 1.0)."""
+    if lib(which).oracle_params_set_timeskip(C.byref(p), C.c_float(timeskip)) != 0:
+        raise ValueError(f"set_timeskip({timeskip}) failed")
+
+
+def read_specs(path, which: str = "f64") -> np.ndarray:
+    """The mat_specs records as loadMaterials reads them: (256, 4) float32
+    rows (sigma, eps_s, eps_i, tau) indexed by class code."""
+    specs = np.zeros((SPEC_CODES, 4), np.float32)
+    rc = lib(which).oracle_read_specs(str(path).encode(), _ptr(specs))
+    if rc != 0:
+        raise ValueError(f"read_specs({path}) failed: {rc}")
+    return specs
+
+
+def threads(cfg: "OracleCfg", which: str = "f64") -> int:
+    """Host threads the oracle's loops run on for cfg."""
+    return int(lib(which).oracle_threads(C.byref(cfg)))
+
+
 def setup_sources(p: OracleParams, which: str = "f64") -> np.ndarray:
     jz = np.zeros(JZ_LEN, np.float32)
     if which == "ref":

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in this directory from the reference itself.
 
-Run in a container that holds the reference sources (``FDTD_REFERENCE_ROOT``,
-default /root/reference): ``python tests/golden/make_golden.py``.  It builds
+Run where the reference sources are, naming their directory:
+``FDTD_REFERENCE_ROOT=<dir> python tests/golden/make_golden.py``.  It builds
 oracle/_ref (the reference's own host code and its kernels compiled for the
 CPU) and records their outputs on synthetic inputs:
 
@@ -30,6 +30,11 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 sys.path.insert(0, str(ROOT))
+
+import os  # noqa: E402
+
+if not os.environ.get("FDTD_REFERENCE_ROOT"):
+    raise SystemExit("set FDTD_REFERENCE_ROOT to the directory holding the reference sources")
 
 from fdtd_gb300 import phantom as ph  # noqa: E402
 from oracle import pyoracle as po  # noqa: E402
