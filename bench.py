@@ -80,7 +80,8 @@ def parse_args():
     ap.add_argument("--timeskip", type=float, default=0.99, help="dt as a fraction of the Courant limit")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-forms", action="store_true", help="skip the compact-form line of the default run")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the other forms (compact, 16-bit, batched, served) of the default run")
     ap.add_argument("--workload", choices=["phantom", "batch", "serve"], default="phantom",
                     help="phantom: the 512x512x400 solve (default); batch: 64 uneven solves in one batch; "
                          "serve: a Poisson request stream through the serving loop")
@@ -98,6 +99,10 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU baseline sample length")
     ap.add_argument("--ref-seconds", type=float, default=150.0,
                     help="--impl reference: most seconds of timed CPU steps (fewer steps than --steps if needed)")
+    ap.add_argument("--forms-batch-steps", type=int, default=300,
+                    help="timed steps of the batched forms in the default run")
+    ap.add_argument("--forms-serve-seconds", type=float, default=10.0,
+                    help="arrival window of the served form in the default run (20 req/s; 0: skip)")
     ap.add_argument("--no-precision", action="store_true",
                     help="skip the probe/DFT/SAR error of the 16-bit-R form against the D form")
     ap.add_argument("--precision-steps", type=int, default=3000, help="steps of the precision comparison")
@@ -488,6 +493,18 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
         if not args.no_precision:
             forms["compact16"]["precision"] = precision_check(p, codes, specs, local_rank, args.precision_steps,
                                                               args.scheme)
+    # ---- the batched (64 uneven solves, both storage forms) and served
+    # (request stream, 16-bit form) forms, N = 1 only
+    if args.kernel == "single" and not args.no_forms and world == 1:
+        reqs = batch_requests(64)
+        btmp = tempfile.TemporaryDirectory()
+        binputs = _request_inputs(reqs, Path(btmp.name))
+        forms["batch"] = {k: batch_form(k, reqs, binputs, args.warmup, args.forms_batch_steps, True)
+                          for k in ("compact", "compact16")}
+        del binputs
+        btmp.cleanup()
+        if args.forms_serve_seconds > 0:
+            forms["serve"] = serve_form("compact16", 20.0, args.forms_serve_seconds)
 
     # ---- end to end through the C ABI with host buffers (e2e)
     e2e = None
@@ -555,16 +572,17 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
     }
     if forms:
         for f in forms.values():
-            f["roofline_frac"] = f["roofline_achieved_gbs"] / peak
+            if "roofline_achieved_gbs" in f:
+                f["roofline_frac"] = f["roofline_achieved_gbs"] / peak
         line["forms"] = forms
     print(json.dumps(line), flush=True)
 
 
 # ------------------------------------------------------- batched / served
 
-def form_name(args) -> str:
-    return {"compact": "compact form (H, E, R)", "compact16": "compact form with 16-bit R (H, E, R16)"}.get(
-        args.kernel, "D form")
+FORM_NAMES = {"single": "D form", "two_pass": "D form", "compact": "compact form (H, E, R)",
+              "compact16": "compact form with 16-bit R (H, E, R16)"}
+
 
 def _request_inputs(reqs, root: Path, threads: int = 8) -> dict:
     """Inputs of each request (input_params + mat_specs + class volume), built
@@ -580,14 +598,9 @@ def _request_inputs(reqs, root: Path, threads: int = 8) -> dict:
         return dict(ex.map(one, reqs))
 
 
-def run_batch_workload(args) -> None:
-    """64 independent solves, dims log-uniform 48-256 per axis, 1-4 Debye
-    ellipsoids each, source 0.3-3 GHz, 500-3000 steps, corrected scheme, in
-    one batch: persistent kernel over the work list of all solves' tiles,
-    graph-replayed.  value = cell-updates of all solves / device time."""
-    import torch
-
-    import fdtd_gb300 as fg
+def batch_requests(n: int = 64):
+    """The 64-solve batch: dims log-uniform 48-256 per axis, 1-4 Debye
+    ellipsoids each, source U[0.3, 3] GHz, steps U[500, 3000] (seeded)."""
     from fdtd_gb300 import serve as sv
 
     rng = np.random.default_rng(1234)
@@ -596,24 +609,33 @@ def run_batch_workload(args) -> None:
         dims = tuple(int(round(math.exp(rng.uniform(math.log(48), math.log(256))))) for _ in range(3))
         reqs.append(sv.Request(rid, 0.0, dims, float(rng.uniform(3e8, 3e9)), int(rng.integers(500, 3001)),
                                int(rng.integers(1 << 30))))
-    reqs = reqs[:max(1, min(64, args.batch_solves))]
-    tmp = tempfile.TemporaryDirectory()
-    inputs = _request_inputs(reqs, Path(tmp.name))
-    b = fg.Batch(0, KERNELS[args.kernel] if args.kernel != "two_pass" else fg.KERNEL_SINGLE_PASS)
+    return reqs[:max(1, min(64, n))]
+
+
+def batch_form(kernel_name: str, reqs, inputs: dict, warmup: int, steps: int, autotune: bool) -> dict:
+    """All solves in one batch of the given form: warm-up steps, the optional
+    autotuner (its trial steps are real steps, before the timed region), then
+    `steps` timed steps (0: until the last solve ends).  value = cell-updates
+    of all solves in the timed steps / device time of those steps."""
+    import torch
+
+    import fdtd_gb300 as fg
+
+    b = fg.Batch(0, KERNELS[kernel_name])
     ids = []
     for r in reqs:
         p, codes, specs, src = inputs[r.rid]
         ids.append(b.add(p, codes, specs, r.steps, scheme=fg.SCHEME_CORRECTED))
-    warm = max(3, args.warmup)
+    warm = max(3, warmup)
     b.run(warm)
     b.synchronize()
-    zchunk = b.autotune() if args.autotune else 0  # its trial steps are real steps, before the timed region
+    zchunk = b.autotune() if autotune else 0
     pre = [b.steps(i) for i in ids]
     stream = torch.cuda.ExternalStream(b.stream)
     a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     to_run = max(r.steps - d for r, d in zip(reqs, pre))
-    if args.batch_steps > 0:
-        to_run = min(to_run, args.batch_steps)
+    if steps > 0:
+        to_run = min(to_run, steps)
     with ClockSampler(0) as clk:
         torch.cuda.synchronize()
         a.record(stream)
@@ -627,60 +649,80 @@ def run_batch_workload(args) -> None:
     cells = [r.dims[0] * r.dims[1] * r.dims[2] for r in reqs]
     updates = sum(c * (q - d) for c, q, d in zip(cells, post, pre))
     peak, peak_kind = measured_peak_gbs()
-    batch_b = FORM_BYTES[args.kernel if args.kernel in ("compact", "compact16") else "single"]
-    line = {
-        "metric": METRIC, "value": updates / seconds, "unit": "cell-updates/s", "n_gpus": 1,
-        "steps": to_run, "warmup": warm, "ms_per_step": seconds / to_run * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"batch of {len(reqs)} solves, dims log-uniform 48-256 per axis, 1-4 Debye ellipsoids, "
-                               f"source U[0.3,3] GHz, steps U[500,3000], corrected scheme, {form_name(args)}",
-                   "solves": len(reqs), "cells_total": sum(cells), "state_bytes": b.bytes,
-                   "cell_updates": updates, "l2": "state >> 129 MB L2: no flush",
-                   "z_chunk_limit": zchunk or "default (compact 16, D form 64 planes)",
-                   "autotune": "fdtd_batch_autotune before timing (its trial steps are excluded)"
-                               if args.autotune else "off"},
-        "roofline": {"bound": "hbm", "kernel": "batch step (all kernels)",
-                     "achieved": batch_b * updates / seconds / 1e9, "peak": peak, "unit": "GB/s",
-                     "frac": batch_b * updates / seconds / 1e9 / peak, "peak_kind": peak_kind, "traffic": None,
-                     "algorithmic_bytes_per_cell_update": batch_b},
-        "gpu_launches": 3 * to_run, "clocks": clk.summary(), "e2e": None, "cpu_baseline": None,
-    }
+    bpc = FORM_BYTES[kernel_name]
+    out = {"value": updates / seconds, "unit": "cell-updates/s", "steps": to_run, "warmup": warm,
+           "ms_per_step": seconds / to_run * 1e3, "form": FORM_NAMES[kernel_name], "solves": len(reqs),
+           "cells_total": sum(cells), "state_bytes": b.bytes, "cell_updates": updates,
+           "z_chunk_limit": zchunk or "default (compact 16, D form 64 planes)",
+           "autotune": "fdtd_batch_autotune before timing (its trial steps are excluded)" if autotune else "off",
+           "roofline": {"bound": "hbm", "kernel": "batch step (all kernels)", "achieved": bpc * updates / seconds / 1e9,
+                        "peak": peak, "unit": "GB/s", "frac": bpc * updates / seconds / 1e9 / peak,
+                        "peak_kind": peak_kind, "algorithmic_bytes_per_cell_update": bpc},
+           "gpu_launches": 3 * to_run, "clocks": clk.summary()}
     b.close()
-    tmp.cleanup()
-    print(json.dumps(line), flush=True)
+    return out
 
 
-def run_serve_workload(args) -> None:
-    """Poisson request stream (dims log-uniform 64-384 per axis, Debye
+def serve_form(kernel_name: str, rate: float, seconds: float, policy: str = "fifo", max_cells: float = 0.0,
+               inputs_threads: int = 8) -> dict:
+    """A Poisson request stream (dims log-uniform 64-384 per axis, Debye
     ellipsoids, source U[0.3,3] GHz, steps U[500,4000]) through the serving
-    loop: admission against a 150 GB budget, continuous batching, Ez snapshot
-    every 250 steps streamed to the host.  Latency is arrival to completion."""
+    loop: admission against a 150 GB budget, continuous batching, Ez
+    snapshot every 250 steps streamed to the host.  Latency is arrival to
+    completion; request inputs are built before the clock starts (they arrive
+    with the requests)."""
     import fdtd_gb300 as fg
     from fdtd_gb300 import serve as sv
 
-    reqs = sv.poisson_stream(args.serve_rate, args.serve_seconds, seed=7, dims=(64, 384), steps=(500, 4000))
+    reqs = sv.poisson_stream(rate, seconds, seed=7, dims=(64, 384), steps=(500, 4000))
     tmp = tempfile.TemporaryDirectory()
-    inputs = _request_inputs(reqs, Path(tmp.name))
+    inputs = _request_inputs(reqs, Path(tmp.name), inputs_threads)
     snaps = []
     with ClockSampler(0) as clk:
         res = sv.serve(reqs, budget_bytes=150 * 10 ** 9, chunk=25, snapshot_every=250, scheme=fg.SCHEME_CORRECTED,
                        inputs=inputs, on_snapshot=lambda r, step, plane: snaps.append(plane.nbytes),
-                       kernel=KERNELS[args.kernel] if args.kernel != "two_pass" else fg.KERNEL_SINGLE_PASS,
-                       policy=args.serve_policy, max_active_cells=args.serve_max_cells or None)
-    summ = res.summary()
-    line = {
-        "metric": "served cell-updates/s and latency", "value": summ["cell_updates_per_s"],
-        "unit": "cell-updates/s", "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"Poisson stream {args.serve_rate} req/s for {args.serve_seconds} s, dims "
-                               f"log-uniform 64-384, steps U[500,4000], 150 GB budget, Ez snapshot every 250 "
-                               f"steps, corrected scheme, {form_name(args)}", "requests": len(reqs),
-                   "policy": args.serve_policy,
-                   "max_active_cells": args.serve_max_cells or "memory budget only"},
-        "serve": {**summ, "snapshot_bytes": int(sum(snaps)), "snapshots": len(snaps)},
-        "clocks": clk.summary(),
-    }
+                       kernel=KERNELS[kernel_name], policy=policy, max_active_cells=max_cells or None)
     tmp.cleanup()
+    summ = res.summary()
+    return {"value": summ["cell_updates_per_s"], "unit": "cell-updates/s", "form": FORM_NAMES[kernel_name],
+            "stream": f"Poisson {rate} req/s for {seconds} s, dims log-uniform 64-384, steps U[500,4000], 150 GB "
+                      f"budget, Ez snapshot every 250 steps (pinned copies on the batch stream), corrected scheme",
+            "requests": len(reqs), "policy": policy, "max_active_cells": max_cells or "memory budget only",
+            "serve": {**summ, "snapshot_bytes": int(sum(snaps)), "snapshots": len(snaps)},
+            "clocks": clk.summary()}
+
+
+def run_batch_workload(args) -> None:
+    """--workload batch: the 64-solve batch in the --kernel form, one line."""
+    reqs = batch_requests(args.batch_solves)
+    tmp = tempfile.TemporaryDirectory()
+    inputs = _request_inputs(reqs, Path(tmp.name))
+    kname = args.kernel if args.kernel in ("compact", "compact16") else "single"
+    f = batch_form(kname, reqs, inputs, args.warmup, args.batch_steps, args.autotune)
+    tmp.cleanup()
+    line = {
+        "metric": METRIC, "value": f["value"], "unit": "cell-updates/s", "n_gpus": 1, "steps": f["steps"],
+        "warmup": f["warmup"], "ms_per_step": f["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"batch of {len(reqs)} solves, dims log-uniform 48-256 per axis, 1-4 Debye "
+                               f"ellipsoids, source U[0.3,3] GHz, steps U[500,3000], corrected scheme, {f['form']}",
+                   **{k: f[k] for k in ("solves", "cells_total", "state_bytes", "cell_updates", "z_chunk_limit",
+                                        "autotune")}, "l2": "state >> 129 MB L2: no flush"},
+        "roofline": {**f["roofline"], "traffic": None}, "gpu_launches": f["gpu_launches"], "clocks": f["clocks"],
+        "e2e": None, "cpu_baseline": None}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve_workload(args) -> None:
+    """--workload serve: the request stream in the --kernel form, one line."""
+    kname = args.kernel if args.kernel in ("compact", "compact16") else "single"
+    f = serve_form(kname, args.serve_rate, args.serve_seconds, args.serve_policy, args.serve_max_cells)
+    line = {"metric": "served cell-updates/s and latency", "value": f["value"], "unit": "cell-updates/s",
+            "n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"{f['stream']}, {f['form']}", "requests": f["requests"], "policy": f["policy"],
+                       "max_active_cells": f["max_active_cells"]},
+            "serve": f["serve"], "clocks": f["clocks"]}
     print(json.dumps(line), flush=True)
 
 

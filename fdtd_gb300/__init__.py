@@ -34,6 +34,7 @@ FDTD_ERR_NO_SYMBOLS = 10004
 FDTD_ERR_NOMEM = 10005
 FDTD_ERR_STATE = 10006
 FDTD_ERR_DEVICE_TIMEOUT = 10007
+FDTD_ERR_BUSY = 10008
 MAX_SOURCES = 16
 JZ_LEN = 65536
 MAX_CLASSES = 256
@@ -162,6 +163,7 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_solver_get_dft", _I, _V, _I, C.POINTER(C.c_double), C.POINTER(C.c_double))
         _sig(L, "fdtd_solver_peak_sar", _I, _V, _P, C.POINTER(C.c_double), C.POINTER(C.c_longlong))
         _sig(L, "fdtd_solver_kernel_name", C.c_char_p, _V, _I)
+        _sig(L, "fdtd_solver_memless_fraction", C.c_double, _V)
         _sig(L, "fdtd_batch_create", _I, _I, C.POINTER(_V))
         _sig(L, "fdtd_batch_create_form", _I, _I, _I, C.POINTER(_V))
         _sig(L, "fdtd_batch_need_bytes", C.c_size_t, _V, _I, _I, _I)
@@ -177,6 +179,13 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_batch_bytes", C.c_size_t, _V)
         _sig(L, "fdtd_batch_size", _I, _V)
         _sig(L, "fdtd_batch_stream", _V, _V)
+        _sig(L, "fdtd_batch_read_async", _I, _V, _I, _I, _I, _I, _V, C.POINTER(C.c_longlong))
+        _sig(L, "fdtd_batch_mark", _I, _V, C.POINTER(C.c_longlong))
+        _sig(L, "fdtd_batch_ticket", _I, _V, C.c_longlong, _I)
+        _sig(L, "fdtd_batch_set_timing", _I, _V, _I)
+        _sig(L, "fdtd_batch_busy", _I, _V, C.POINTER(C.c_double), C.POINTER(C.c_double))
+        _sig(L, "fdtd_host_alloc", _I, C.c_size_t, C.POINTER(_V))
+        _sig(L, "fdtd_host_free", _I, _V)
         _LIB = L
     return _LIB
 
@@ -386,6 +395,12 @@ class Solver:
         check(lib().fdtd_solver_profile(self.handle, nsteps, ms, 8, C.byref(nk)), "fdtd_solver_profile")
         return {lib().fdtd_solver_kernel_name(self.handle, k).decode(): float(ms[k]) for k in range(nk.value)}
 
+    @property
+    def memless_fraction(self) -> float:
+        """Compact forms: share of the cell-updates on tile-planes without Debye
+        memory, whose R the step kernel skips."""
+        return lib().fdtd_solver_memless_fraction(self.handle)
+
     def checkpoint(self, path) -> None:
         check(lib().fdtd_solver_checkpoint(self.handle, str(path).encode()), "fdtd_solver_checkpoint")
 
@@ -515,6 +530,43 @@ class Batch:
         names = [n for n in FIELDS if not (self.kernel in COMPACT_KERNELS and n.startswith("d"))]
         return {n: self.field(sid, n) for n in names}
 
+    def read_async(self, sid: int, name: str, out: np.ndarray, z0: int = 0, nplanes: int = 0) -> int:
+        """Queues a copy of planes [z0, z0 + nplanes) of a field, as it will be
+        after the steps queued so far, into out (float32, (nplanes, ny, nx);
+        page-locked for an asynchronous copy, e.g. PinnedBuffer); returns a
+        ticket for done().  out must stay alive until then."""
+        nz, ny, nx = self._keep[sid][1]
+        n = nplanes or nz
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size >= n * ny * nx
+        t = C.c_longlong()
+        check(lib().fdtd_batch_read_async(self.handle, sid, FIELD_ID[name], z0, nplanes,
+                                          out.ctypes.data_as(C.c_void_p), C.byref(t)), "fdtd_batch_read_async")
+        return t.value
+
+    def mark(self) -> int:
+        """A ticket for the point after everything queued so far."""
+        t = C.c_longlong()
+        check(lib().fdtd_batch_mark(self.handle, C.byref(t)), "fdtd_batch_mark")
+        return t.value
+
+    def done(self, ticket: int, wait: bool = False) -> bool:
+        """Whether the ticket's work has finished (the ticket is then spent)."""
+        st = lib().fdtd_batch_ticket(self.handle, ticket, 1 if wait else 0)
+        if st == FDTD_ERR_BUSY:
+            return False
+        check(st, "fdtd_batch_ticket")
+        return True
+
+    def set_timing(self, on: bool = True) -> None:
+        check(lib().fdtd_batch_set_timing(self.handle, 1 if on else 0), "fdtd_batch_set_timing")
+
+    def busy(self) -> tuple[float, float]:
+        """(GPU ms of the finished timed runs, ms from the first run's start to
+        the last finished run's end)."""
+        b, s = C.c_double(), C.c_double()
+        check(lib().fdtd_batch_busy(self.handle, C.byref(b), C.byref(s)), "fdtd_batch_busy")
+        return b.value, s.value
+
     @property
     def bytes(self) -> int:
         return lib().fdtd_batch_bytes(self.handle)
@@ -530,6 +582,33 @@ class Batch:
         if getattr(self, "handle", None):
             lib().fdtd_batch_destroy(self.handle)
             self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host memory (fdtd_host_alloc) viewed as a float32 array,
+    for asynchronous device-to-host copies."""
+
+    def __init__(self, nfloats: int):
+        p = C.c_void_p()
+        check(lib().fdtd_host_alloc(4 * nfloats, C.byref(p)), "fdtd_host_alloc")
+        self._ptr = p
+        self.array = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_float)), shape=(nfloats,))
+
+    def view(self, shape) -> np.ndarray:
+        n = int(np.prod(shape))
+        return self.array[:n].reshape(shape)
+
+    def close(self) -> None:
+        if getattr(self, "_ptr", None):
+            self.array = None
+            lib().fdtd_host_free(self._ptr)
+            self._ptr = None
 
     def __del__(self):
         try:

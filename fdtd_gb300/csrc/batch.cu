@@ -12,7 +12,17 @@
 // captured graph serves every step; a solve stops once it reaches its target
 // step count.  Adding or removing a solve rebuilds the descriptors and the
 // graph.  No reference counterpart (the reference runs one grid).
+//
+// Nothing on the way of a running batch waits for the GPU: a new solve's
+// memory comes from the batch's stream-ordered pool and its uploads run on a
+// side stream (the batch stream waits for them before the solve's first
+// step); descriptor uploads go through pinned staging buffers; a removed
+// solve's memory is freed in stream order behind the work that reads it; and
+// field reads can be queued as copies into the caller's host memory, with a
+// ticket to poll.  A serving loop can so admit, snapshot and retire solves
+// while earlier batched steps still run.
 #include <algorithm>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -39,6 +49,8 @@ struct BatchSolve {
     uint8_t *mat = nullptr;
     uint32_t *rexp = nullptr;  // 16-bit R form: scale words
     int *counter = nullptr;
+    int host_steps = 0;              // steps queued for this solve so far (its counter once they ran)
+    cudaEvent_t ready = nullptr;     // its uploads on the side stream; waited for before its first step
 };
 
 size_t padded_pitch(int nx) { return ((size_t)nx + 15) & ~size_t(15); }
@@ -63,11 +75,29 @@ size_t plan_bytes(int nx, int ny, int nz)
 
 }  // namespace
 
+// Pinned host buffer for descriptor uploads; done marks the end of its last upload.
+struct StageBuf {
+    void *host = nullptr;
+    size_t cap = 0;
+    cudaEvent_t done = nullptr;
+};
+
 struct fdtd_batch {
     int device = 0;
     bool compact = false;  // every solve keeps the compact state
     bool r16 = false;      // ... with R in 16 bits
     cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;      // uploads of solves being added
+    cudaMemPool_t pool = nullptr;     // device memory of the solves, descriptors and Mur blocks
+    StageBuf stage[2];                // alternating pinned staging of descriptor uploads
+    int stage_next = 0;
+    std::vector<cudaEvent_t> spare_events;
+    std::map<long long, cudaEvent_t> tickets;  // queued reads and marks
+    long long next_ticket = 1;
+    bool timing = false;              // events around every fdtd_batch_run (busy time)
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> runs;
+    double busy_ms = 0.0, span_ms = 0.0;
+    cudaEvent_t first_start = nullptr;
     std::vector<BatchSolve *> solves;
     int next_id = 1;
     bool dirty = true;
@@ -84,13 +114,80 @@ struct fdtd_batch {
 
 namespace {
 
-void free_solve(BatchSolve *v)
+// Frees a solve in stream order on s (behind the work queued there).
+void free_solve(BatchSolve *v, cudaStream_t s)
 {
     if (!v)
         return;
-    cudaFree(v->d_block);
-    fdtd_plan_destroy(v->plan);
+    if (v->d_block)
+        cudaFreeAsync(v->d_block, s);
+    plan_destroy_on(v->plan, s);
+    if (v->ready)
+        cudaEventDestroy(v->ready);
     delete v;
+}
+
+cudaEvent_t take_event(fdtd_batch *b)
+{
+    if (!b->spare_events.empty()) {
+        cudaEvent_t e = b->spare_events.back();
+        b->spare_events.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    return cudaEventCreate(&e) == cudaSuccess ? e : nullptr;
+}
+
+// Device memory from the batch's pool, in stream order on s.
+int pool_alloc(fdtd_batch *b, void **p, size_t bytes, cudaStream_t s)
+{
+    return cu(cudaMallocFromPoolAsync(p, bytes, b->pool, s));
+}
+
+// Copies n bytes of host data to dst on the batch stream through the next
+// pinned staging buffer (waiting only for that buffer's previous upload).
+int staged_upload(fdtd_batch *b, void *dst, const void *src, size_t n)
+{
+    StageBuf &sb = b->stage[b->stage_next];
+    b->stage_next ^= 1;
+    int st = cu(cudaEventSynchronize(sb.done));
+    if (st == FDTD_OK && sb.cap < n) {
+        if (sb.host)
+            cudaFreeHost(sb.host);
+        sb.host = nullptr;
+        sb.cap = 0;
+        const size_t cap = std::max(n, size_t(1) << 20);
+        st = cu(cudaHostAlloc(&sb.host, cap, cudaHostAllocDefault));
+        if (st == FDTD_OK)
+            sb.cap = cap;
+    }
+    if (st == FDTD_OK) {
+        std::memcpy(sb.host, src, n);
+        st = cu(cudaMemcpyAsync(dst, sb.host, n, cudaMemcpyHostToDevice, b->stream));
+    }
+    if (st == FDTD_OK)
+        st = cu(cudaEventRecord(sb.done, b->stream));
+    return st;
+}
+
+// Busy time of the completed timed runs (in order), added to b's totals.
+void collect_runs(fdtd_batch *b)
+{
+    size_t k = 0;
+    for (; k < b->runs.size(); k++) {
+        auto &r = b->runs[k];
+        if (cudaEventQuery(r.second) != cudaSuccess)
+            break;
+        float ms = 0.0f, span = 0.0f;
+        cudaEventElapsedTime(&ms, r.first, r.second);
+        b->busy_ms += ms;
+        cudaEventElapsedTime(&span, b->first_start, r.second);
+        b->span_ms = span;
+        if (r.first != b->first_start)
+            b->spare_events.push_back(r.first);
+        b->spare_events.push_back(r.second);
+    }
+    b->runs.erase(b->runs.begin(), b->runs.begin() + k);
 }
 
 void drop_graphs(fdtd_batch *b)
@@ -100,7 +197,7 @@ void drop_graphs(fdtd_batch *b)
     b->graphs.clear();
 }
 
-NativeConsts solve_consts(const BatchSolve *v, int parity)
+NativeConsts solve_consts(const BatchSolve *v, int parity, int *err)
 {
     fdtd_native_fields f{};
     const int cur = (parity + 1) & 1, prv = parity & 1;
@@ -117,8 +214,12 @@ NativeConsts solve_consts(const BatchSolve *v, int parity)
     c.pitch = v->pitch;
     c.step_counter = v->counter;
     c.r_exp = v->rexp;
+    c.err = err;  // one error word for the batch
     return c;
 }
+
+// Word of the batch's work buffer that a bounded wait which gave up sets.
+constexpr int BATCH_ERR_WORD = 32;
 
 int rebuild(fdtd_batch *b)
 {
@@ -131,7 +232,7 @@ int rebuild(fdtd_batch *b)
         BatchDesc &d = descs[i];
         std::memset(&d, 0, sizeof d);
         for (int par = 0; par < 2; par++) {
-            d.c[par] = solve_consts(v, par);
+            d.c[par] = solve_consts(v, par, b->d_work + BATCH_ERR_WORD);
             if (!encode_step_maps(d.c[par], b->compact, &d.maps[par], b->r16))
                 return FDTD_ERR_INVALID;
         }
@@ -151,27 +252,36 @@ int rebuild(fdtd_batch *b)
                 mur.push_back(BatchMurBlock{(int)i, f, (int)first, 0});
         }
     }
+    // new solves: the batch stream waits for their uploads on the side stream
     int st = FDTD_OK;
-    if (descs.size() > b->descs_cap) {
-        cudaFree(b->d_descs);
+    for (auto *v : b->solves)
+        if (v->ready && st == FDTD_OK) {
+            st = cu(cudaStreamWaitEvent(b->stream, v->ready, 0));
+            cudaEventDestroy(v->ready);
+            v->ready = nullptr;
+        }
+    // device tables grow in stream order (the old ones are freed behind the
+    // steps that still read them)
+    if (st == FDTD_OK && descs.size() > b->descs_cap) {
+        if (b->d_descs)
+            cudaFreeAsync(b->d_descs, b->stream);
         b->d_descs = nullptr;
-        st = cu(cudaMalloc(&b->d_descs, sizeof(BatchDesc) * descs.size()));
-        b->descs_cap = st == FDTD_OK ? descs.size() : 0;
+        const size_t cap = std::max(descs.size() * 2, size_t(16));
+        st = pool_alloc(b, reinterpret_cast<void **>(&b->d_descs), sizeof(BatchDesc) * cap, b->stream);
+        b->descs_cap = st == FDTD_OK ? cap : 0;
     }
     if (st == FDTD_OK && mur.size() > b->mur_cap) {
-        cudaFree(b->d_mur);
+        if (b->d_mur)
+            cudaFreeAsync(b->d_mur, b->stream);
         b->d_mur = nullptr;
-        st = cu(cudaMalloc(&b->d_mur, sizeof(BatchMurBlock) * mur.size()));
-        b->mur_cap = st == FDTD_OK ? mur.size() : 0;
+        const size_t cap = std::max(mur.size() * 2, size_t(1024));
+        st = pool_alloc(b, reinterpret_cast<void **>(&b->d_mur), sizeof(BatchMurBlock) * cap, b->stream);
+        b->mur_cap = st == FDTD_OK ? cap : 0;
     }
     if (st == FDTD_OK && !descs.empty())
-        st = cu(cudaMemcpyAsync(b->d_descs, descs.data(), sizeof(BatchDesc) * descs.size(), cudaMemcpyHostToDevice,
-                                b->stream));
+        st = staged_upload(b, b->d_descs, descs.data(), sizeof(BatchDesc) * descs.size());
     if (st == FDTD_OK && !mur.empty())
-        st = cu(cudaMemcpyAsync(b->d_mur, mur.data(), sizeof(BatchMurBlock) * mur.size(), cudaMemcpyHostToDevice,
-                                b->stream));
-    if (st == FDTD_OK)
-        st = cu(cudaStreamSynchronize(b->stream));
+        st = staged_upload(b, b->d_mur, mur.data(), sizeof(BatchMurBlock) * mur.size());
     if (st != FDTD_OK)
         return st;
     int max_classes = 1;
@@ -273,6 +383,23 @@ int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out)
     b->r16 = kernel == FDTD_KERNEL_COMPACT_R16;
     st = cu(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
     if (st == FDTD_OK)
+        st = cu(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+    if (st == FDTD_OK) {
+        // the batch's own pool keeps freed memory for the next solves
+        // instead of returning it to the driver
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = device;
+        st = cu(cudaMemPoolCreate(&b->pool, &props));
+        if (st == FDTD_OK) {
+            uint64_t keep = UINT64_MAX;
+            st = cu(cudaMemPoolSetAttribute(b->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        }
+    }
+    for (int k = 0; k < 2 && st == FDTD_OK; k++)
+        st = cu(cudaEventCreateWithFlags(&b->stage[k].done, cudaEventDisableTiming));
+    if (st == FDTD_OK)
         st = cu(cudaMalloc(&b->d_work, 256));
     if (st == FDTD_OK)
         st = cu(cudaMemset(b->d_work, 0, 256));
@@ -289,14 +416,42 @@ int fdtd_batch_destroy(fdtd_batch *b)
     if (!b)
         return FDTD_OK;
     cudaSetDevice(b->device);
+    if (b->side)
+        cudaStreamSynchronize(b->side);
     if (b->stream)
         cudaStreamSynchronize(b->stream);
     drop_graphs(b);
+    cudaStream_t s = b->stream ? b->stream : b->side;
     for (auto *v : b->solves)
-        free_solve(v);
-    cudaFree(b->d_descs);
-    cudaFree(b->d_mur);
+        free_solve(v, s);
+    if (b->d_descs)
+        cudaFreeAsync(b->d_descs, s);
+    if (b->d_mur)
+        cudaFreeAsync(b->d_mur, s);
+    if (s)
+        cudaStreamSynchronize(s);
     cudaFree(b->d_work);
+    for (auto &sb : b->stage) {
+        if (sb.host)
+            cudaFreeHost(sb.host);
+        if (sb.done)
+            cudaEventDestroy(sb.done);
+    }
+    for (auto &kv : b->tickets)
+        cudaEventDestroy(kv.second);
+    for (auto &r : b->runs) {
+        if (r.first != b->first_start)
+            cudaEventDestroy(r.first);
+        cudaEventDestroy(r.second);
+    }
+    if (b->first_start)
+        cudaEventDestroy(b->first_start);
+    for (auto e : b->spare_events)
+        cudaEventDestroy(e);
+    if (b->pool)
+        cudaMemPoolDestroy(b->pool);
+    if (b->side)
+        cudaStreamDestroy(b->side);
     if (b->stream)
         cudaStreamDestroy(b->stream);
     delete b;
@@ -316,8 +471,6 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
             return FDTD_ERR_INVALID;
     }
     int st = cu(cudaSetDevice(b->device));
-    if (st == FDTD_OK)
-        st = cu(cudaStreamSynchronize(b->stream));
     if (st != FDTD_OK)
         return st;
     if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, nullptr) != FDTD_OK)
@@ -329,14 +482,16 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
     v->pitch = (int)padded_pitch(p->nx);
     v->ncell = (size_t)v->pitch * v->ny * v->nz;
     v->steps_target = steps;
-    st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &v->plan);
+    // everything of the new solve goes on the side stream: the batch stream
+    // keeps running the steps already queued
+    st = plan_create_on(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, b->pool, b->side, &v->plan);
     const size_t fbytes = (v->ncell * sizeof(float) + 255) & ~size_t(255);
     const size_t total = state_bytes(p->nx, p->ny, p->nz, b->compact, b->r16);
     const size_t dbytes = b->r16 ? r16_array_bytes(v->ncell) : fbytes;
     if (st == FDTD_OK)
-        st = cu(cudaMalloc(&v->d_block, total));
+        st = pool_alloc(b, reinterpret_cast<void **>(&v->d_block), total, b->side);
     if (st == FDTD_OK)
-        st = cu(cudaMemsetAsync(v->d_block, 0, total, b->stream));
+        st = cu(cudaMemsetAsync(v->d_block, 0, total, b->side));
     if (st == FDTD_OK) {
         char *q = v->d_block;
         for (int s = 0; s < 2; s++)
@@ -361,12 +516,17 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         v->counter = reinterpret_cast<int *>(q);
         // dense host classes -> padded rows (one 2-D copy per z plane range)
         st = cu(cudaMemcpy2DAsync(v->mat, v->pitch, cfg->material, p->nx, p->nx, (size_t)p->ny * p->nz,
-                                  cudaMemcpyHostToDevice, b->stream));
+                                  cudaMemcpyHostToDevice, b->side));
     }
     if (st == FDTD_OK)
-        st = cu(cudaStreamSynchronize(b->stream));
+        st = cu(cudaEventCreateWithFlags(&v->ready, cudaEventDisableTiming));
+    if (st == FDTD_OK)
+        st = cu(cudaEventRecord(v->ready, b->side));
+    // the caller's class volume may go once the copy has read it
+    if (st == FDTD_OK)
+        st = cu(cudaStreamSynchronize(b->side));
     if (st != FDTD_OK) {
-        free_solve(v);
+        free_solve(v, b->side);
         return st;
     }
     v->bytes = total + plan_bytes(p->nx, p->ny, p->nz);
@@ -385,11 +545,13 @@ int fdtd_batch_remove(fdtd_batch *b, int id)
     BatchSolve *v = find(b, id);
     if (!v)
         return FDTD_ERR_INVALID;
-    cudaSetDevice(b->device);
-    const int st = cu(cudaStreamSynchronize(b->stream));
+    const int st = cu(cudaSetDevice(b->device));
     b->solves.erase(std::find(b->solves.begin(), b->solves.end(), v));
     b->bytes -= v->bytes;
-    free_solve(v);
+    if (v->ready) {  // never stepped: its uploads are ordered before the free
+        cudaStreamWaitEvent(b->stream, v->ready, 0);
+    }
+    free_solve(v, b->stream);  // behind the queued steps and reads
     b->dirty = true;
     return st;
 }
@@ -403,7 +565,21 @@ int fdtd_batch_run(fdtd_batch *b, int nsteps)
         return st;
     if (b->dirty && (st = rebuild(b)) != FDTD_OK)
         return st;
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    if (b->timing) {
+        t0 = b->first_start ? take_event(b) : nullptr;
+        if (!b->first_start) {
+            st = cu(cudaEventCreate(&b->first_start));
+            t0 = b->first_start;
+        }
+        t1 = take_event(b);
+        if (st == FDTD_OK && (!t0 || !t1))
+            st = FDTD_ERR_NOMEM;
+        if (st == FDTD_OK)
+            st = cu(cudaEventRecord(t0, b->stream));
+    }
     const int chunk = 8;
+    const int total = nsteps;
     while (nsteps > 0 && st == FDTD_OK) {
         const int len = nsteps >= chunk ? chunk : 1;
         cudaGraphExec_t g;
@@ -412,6 +588,14 @@ int fdtd_batch_run(fdtd_batch *b, int nsteps)
             st = cu(cudaGraphLaunch(g, b->stream));
         nsteps -= len;
     }
+    if (b->timing && st == FDTD_OK) {
+        st = cu(cudaEventRecord(t1, b->stream));
+        if (st == FDTD_OK)
+            b->runs.emplace_back(t0, t1);
+    }
+    if (st == FDTD_OK)
+        for (auto *v : b->solves)
+            v->host_steps = std::min(v->steps_target, v->host_steps + total);
     return st;
 }
 
@@ -479,10 +663,112 @@ int fdtd_batch_synchronize(fdtd_batch *b)
         return FDTD_ERR_INVALID;
     cudaSetDevice(b->device);
     int st = cu(cudaStreamSynchronize(b->stream));
-    for (auto *v : b->solves)
-        if (st == FDTD_OK)
-            st = plan_error(v->plan);
+    int flag = 0;
+    if (st == FDTD_OK)
+        st = cu(cudaMemcpy(&flag, b->d_work + BATCH_ERR_WORD, sizeof flag, cudaMemcpyDeviceToHost));
+    if (st == FDTD_OK && flag) {
+        cudaMemset(b->d_work + BATCH_ERR_WORD, 0, sizeof flag);
+        st = FDTD_ERR_DEVICE_TIMEOUT;
+    }
+    if (b->timing)
+        collect_runs(b);
     return st;
+}
+
+int fdtd_batch_read_async(fdtd_batch *b, int id, int field, int z0, int nplanes, float *host_out,
+                          long long *ticket)
+{
+    if (!b || !host_out || !ticket || field < 0 || field >= FDTD_FIELD_COUNT)
+        return FDTD_ERR_INVALID;
+    BatchSolve *v = find(b, id);
+    if (!v)
+        return FDTD_ERR_INVALID;
+    if (nplanes == 0) {
+        z0 = 0;
+        nplanes = v->nz;
+    }
+    if (z0 < 0 || nplanes < 0 || z0 + nplanes > v->nz)
+        return FDTD_ERR_INVALID;
+    if (b->compact && field >= FDTD_FIELD_DX && field <= FDTD_FIELD_DZ)
+        return FDTD_ERR_INVALID;  // D is not stored
+    int st = cu(cudaSetDevice(b->device));
+    if (st != FDTD_OK)
+        return st;
+    if (v->ready) {  // queued before the solve's first step: its uploads come first
+        st = cu(cudaStreamWaitEvent(b->stream, v->ready, 0));
+        if (st != FDTD_OK)
+            return st;
+    }
+    // the slots as they are after the steps queued so far
+    const int n = v->host_steps, comp = field % 3;
+    const float *src;
+    if (field < 3)
+        src = v->h[n & 1][comp];
+    else {
+        const int slot = n > 0 ? ((n - 1) & 1) : 0;
+        src = field < 6 ? v->d[slot][comp] : v->e[slot][comp];
+    }
+    src += (size_t)z0 * v->pitch * v->ny;
+    st = cu(cudaMemcpy2DAsync(host_out, sizeof(float) * v->nx, src, sizeof(float) * v->pitch, sizeof(float) * v->nx,
+                              (size_t)v->ny * nplanes, cudaMemcpyDeviceToHost, b->stream));
+    if (st != FDTD_OK)
+        return st;
+    return fdtd_batch_mark(b, ticket);
+}
+
+int fdtd_batch_mark(fdtd_batch *b, long long *ticket)
+{
+    if (!b || !ticket)
+        return FDTD_ERR_INVALID;
+    cudaSetDevice(b->device);
+    cudaEvent_t e = take_event(b);
+    if (!e)
+        return FDTD_ERR_NOMEM;
+    const int st = cu(cudaEventRecord(e, b->stream));
+    if (st != FDTD_OK) {
+        b->spare_events.push_back(e);
+        return st;
+    }
+    *ticket = b->next_ticket++;
+    b->tickets[*ticket] = e;
+    return FDTD_OK;
+}
+
+int fdtd_batch_ticket(fdtd_batch *b, long long ticket, int wait)
+{
+    if (!b)
+        return FDTD_ERR_INVALID;
+    auto it = b->tickets.find(ticket);
+    if (it == b->tickets.end())
+        return FDTD_ERR_INVALID;
+    cudaSetDevice(b->device);
+    const cudaError_t e = wait ? cudaEventSynchronize(it->second) : cudaEventQuery(it->second);
+    if (e == cudaErrorNotReady)
+        return FDTD_ERR_BUSY;
+    b->spare_events.push_back(it->second);
+    b->tickets.erase(it);
+    if (b->timing)
+        collect_runs(b);
+    return cu(e);
+}
+
+int fdtd_batch_set_timing(fdtd_batch *b, int on)
+{
+    if (!b)
+        return FDTD_ERR_INVALID;
+    b->timing = on != 0;
+    return FDTD_OK;
+}
+
+int fdtd_batch_busy(fdtd_batch *b, double *busy_ms, double *span_ms)
+{
+    if (!b || !busy_ms || !span_ms)
+        return FDTD_ERR_INVALID;
+    cudaSetDevice(b->device);
+    collect_runs(b);
+    *busy_ms = b->busy_ms;
+    *span_ms = b->span_ms;
+    return FDTD_OK;
 }
 
 int fdtd_batch_steps(fdtd_batch *b, int id)

@@ -36,7 +36,7 @@ const char *cuda_error_string(int code);
 // which is exact algebra for the reference's k1 = 2 fl(dt + tau),
 // k2 = 2 dt + 4 tau, k3 = 2 tau and avoids the cancellation of the three
 // large products in single precision.
-struct DebyeCoef {
+struct alignas(16) DebyeCoef {
     float a, c, d, two_dt, two_tau, delta, pad0, pad1;
 };
 static_assert(sizeof(DebyeCoef) == 32, "DebyeCoef is two float4");

@@ -85,6 +85,7 @@ const char *fdtd_status_string(int status)
     case FDTD_ERR_NOMEM: return "host allocation failed";
     case FDTD_ERR_STATE: return "call not valid in the current state";
     case FDTD_ERR_DEVICE_TIMEOUT: return "a kernel gave up a bounded wait; results are invalid";
+    case FDTD_ERR_BUSY: return "the queued work has not finished yet";
     default: return cuda_error_string(status);
     }
 }

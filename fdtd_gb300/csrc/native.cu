@@ -325,6 +325,16 @@ extern "C" {
 int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int scheme,
                      const float *const rp_host[6], fdtd_plan **out)
 {
+    return plan_create_on(p, specs, nclasses, scheme, rp_host, nullptr, nullptr, out);
+}
+
+}  // extern "C"
+
+namespace fdtd {
+
+int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int scheme, const float *const rp_host[6],
+                   cudaMemPool_t pool, cudaStream_t stream, fdtd_plan **out)
+{
     if (!p || !specs || !out || nclasses < 1 || nclasses > FDTD_MAX_CLASSES || p->nx < 3 || p->ny < 3 ||
         p->nz < 3 || p->nz > 65535 || p->sourcesCount < 0 || p->sourcesCount > FDTD_MAX_SOURCES ||
         (scheme != FDTD_SCHEME_REFERENCE && scheme != FDTD_SCHEME_CORRECTED))
@@ -406,12 +416,20 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
     const size_t err_off = cur;
     total = cur + 256;
     char *base = nullptr;
-    cudaError_t e = cudaMalloc(&base, total);
+    cudaError_t e = pool ? cudaMallocFromPoolAsync(reinterpret_cast<void **>(&base), total, pool, stream)
+                         : cudaMalloc(&base, total);
     if (e != cudaSuccess) {
         delete plan;
         return e;
     }
     plan->d_block = base;
+    plan->pooled = pool != nullptr;
+    // copies: blocking ones, or (pool) ones ordered on the stream that the
+    // caller synchronises before the host vectors below go away
+    auto put = [&](void *dst, const void *src, size_t n) {
+        return pool ? cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, stream)
+                    : cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
+    };
     plan->d_coef = reinterpret_cast<DebyeCoef *>(base + offs[0]);
     plan->d_jz = reinterpret_cast<float *>(base + offs[1]);
     float *rpd[6];
@@ -443,18 +461,24 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
                     murx[((size_t)face * p->nz + z) * p->ny + y] = v;
                 }
         }
-        e = cudaMemcpy(plan->d_mur_x, murx.data(), sizeof(float4) * nmurx, cudaMemcpyHostToDevice);
+        e = put(plan->d_mur_x, murx.data(), sizeof(float4) * nmurx);
+        if (e == cudaSuccess)  // error flag, test hook word
+            e = pool ? cudaMemsetAsync(plan->d_err, 0, 2 * sizeof(int), stream)
+                     : cudaMemset(plan->d_err, 0, 2 * sizeof(int));
+        if (e == cudaSuccess)
+            e = put(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES);
+        if (e == cudaSuccess)
+            e = put(plan->d_jz, jz.data(), sizeof(float) * FDTD_JZ_LEN);
+        for (int k = 0; k < 6 && e == cudaSuccess; k++)
+            e = put(rpd[k], rp[k].data(), sizeof(float) * nrp[k]);
+        if (pool && e == cudaSuccess)
+            e = cudaStreamSynchronize(stream);  // the host vectors are released below
     }
-    if (e == cudaSuccess)
-        e = cudaMemset(plan->d_err, 0, 2 * sizeof(int));  // error flag, test hook word
-    if (e == cudaSuccess)
-        e = cudaMemcpy(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(plan->d_jz, jz.data(), sizeof(float) * FDTD_JZ_LEN, cudaMemcpyHostToDevice);
-    for (int k = 0; k < 6 && e == cudaSuccess; k++)
-        e = cudaMemcpy(rpd[k], rp[k].data(), sizeof(float) * nrp[k], cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
-        cudaFree(base);
+        if (pool)
+            cudaFreeAsync(base, stream);
+        else
+            cudaFree(base);
         delete plan;
         return e;
     }
@@ -462,6 +486,21 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
     *out = plan;
     return FDTD_OK;
 }
+
+void plan_destroy_on(fdtd_plan *plan, cudaStream_t stream)
+{
+    if (!plan)
+        return;
+    if (plan->pooled)
+        cudaFreeAsync(plan->d_block, stream);
+    else
+        cudaFree(plan->d_block);
+    delete plan;
+}
+
+}  // namespace fdtd
+
+extern "C" {
 
 int fdtd_plan_status(fdtd_plan *plan)
 {
@@ -477,7 +516,7 @@ int fdtd_plan_destroy(fdtd_plan *plan)
 {
     if (!plan)
         return FDTD_OK;
-    cudaError_t e = cudaFree(plan->d_block);
+    cudaError_t e = plan->pooled ? cudaFreeAsync(plan->d_block, nullptr) : cudaFree(plan->d_block);
     delete plan;
     return e == cudaSuccess ? FDTD_OK : (int)e;
 }

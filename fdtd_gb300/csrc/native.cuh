@@ -24,6 +24,7 @@ struct fdtd_plan {
     float4 *d_mur_x = nullptr;            // x-face Mur coefficients, [face][z][y] (see mur_x_coef)
     int *d_err = nullptr;                 // device error flag
     int *d_stall = nullptr;               // test hook word (NativeConsts::stall_once)
+    bool pooled = false;                  // d_block comes from a stream-ordered pool (plan_create_on)
 };
 
 namespace fdtd {
@@ -64,6 +65,11 @@ struct NativeConsts {
     const float *d_cur[3];
     float *d_prev[3];
     const uint8_t *mat;
+    // compact forms, strip kernel: per unit (tile x, tile y, z chunk) a bit
+    // per plane of the chunk whose tile holds only classes without
+    // relaxation (R stays +0 there: not loaded, not stored); may be null
+    const unsigned long long *memless;
+    int memless_rows;      // tile rows the masks were made for (other tile heights ignore them)
 };
 
 NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n);
@@ -179,7 +185,39 @@ int zchunk_limited(int nz, int max_planes);  // nz in equal chunks of at most ma
 int launch_batch_step(const BatchLaunch &b, cudaStream_t s);
 int batch_persistent_ctas(bool compact, int nclasses, bool r16 = false);
 
+// The compact forms' step kernel with TMA loads and stores over column strips
+// (step_strip.cu); usable when every array is TMA-addressable (rows of a
+// multiple of 16 cells, 16-byte aligned bases, R updated in place).
+bool strip_usable(const NativeConsts &c, bool r16);
+// Strip shapes (0 .. 3) and their tile rows; the shape a single solve runs
+// (FDTD_STRIP_SHAPE overrides); the z chunk of a single solve's strip launch.
+int strip_shape_rows(int shape);
+int strip_single_shape(bool r16);
+int strip_zchunk(int nz);
+// Memoryless tile-planes (see NativeConsts::memless): strip_plane_flags marks
+// each (z, 32 x 8 tile) whose cells all have classes with tau
+// (specs[4 k + 3]) = 0, for a class volume of row pitch `pitch`, laid out
+// [z][tile y][tile x]; strip_unit_masks packs them into one 64-bit word per
+// unit of ty-row tiles (ty a multiple of 8) and z chunks of zchunk planes,
+// units ordered (z chunk, tile y, tile x) with tile x fastest, and returns
+// the fraction of the grid's cells on such planes.
+std::vector<unsigned char> strip_plane_flags(const uint8_t *mat, int nx, int ny, int nz, int pitch, const float *specs,
+                                             int nclasses);
+double strip_unit_masks(const std::vector<unsigned char> &flags, int nx, int ny, int nz, int ty, int zchunk,
+                        unsigned long long *masks);
+int launch_strip_compact(const NativeConsts &c, cudaStream_t s);
+int launch_strip_compact16(const NativeConsts &c, cudaStream_t s);
+
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);
+
+// fdtd_plan_create with the plan's device memory taken from pool in stream
+// order on stream (copies on that stream, which is synchronised before the
+// call returns); with a null pool, as fdtd_plan_create.  plan_destroy_on
+// frees a pooled plan in stream order on stream (no device-wide wait), any
+// other plan as fdtd_plan_destroy does.
+int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int scheme, const float *const rp_host[6],
+                   cudaMemPool_t pool, cudaStream_t stream, fdtd_plan **out);
+void plan_destroy_on(fdtd_plan *plan, cudaStream_t stream);
 
 }  // namespace fdtd

@@ -47,6 +47,8 @@ NativeConsts solver_consts(const fdtd_solver *s, int n)
     const fdtd_native_fields f = step_fields(s, n);
     NativeConsts c = make_consts(s->plan, &f, n);
     c.r_exp = s->rexp;
+    c.memless = s->d_memless;
+    c.memless_rows = s->memless_rows;
     return c;
 }
 
@@ -380,6 +382,23 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         st = cu(cudaMemsetAsync(s->d_block, 0, total, s->stream));
     if (st == FDTD_OK)
         st = cu(cudaMemcpyAsync(s->mat, cfg->material, n, cudaMemcpyHostToDevice, s->stream));
+    if (st == FDTD_OK && stores_no_d(cfg->kernel)) {
+        // tile-planes without Debye memory: the strip kernel skips their R
+        const std::vector<unsigned char> flags =
+            strip_plane_flags(cfg->material, p->nx, p->ny, p->nz, p->nx, cfg->specs, cfg->nclasses);
+        s->memless_rows = strip_shape_rows(strip_single_shape(cfg->kernel == FDTD_KERNEL_COMPACT_R16));
+        const int zchunk = strip_zchunk(p->nz);
+        std::vector<unsigned long long> masks((size_t)((p->nz + zchunk - 1) / zchunk) *
+                                              ((p->ny + s->memless_rows - 1) / s->memless_rows) * ((p->nx + 31) / 32));
+        s->memless_fraction =
+            strip_unit_masks(flags, p->nx, p->ny, p->nz, s->memless_rows, zchunk, masks.data());
+        if (s->memless_fraction > 0.0) {
+            st = cu(cudaMalloc(&s->d_memless, masks.size() * sizeof(unsigned long long)));
+            if (st == FDTD_OK)
+                st = cu(cudaMemcpyAsync(s->d_memless, masks.data(), masks.size() * sizeof(unsigned long long),
+                                        cudaMemcpyHostToDevice, s->stream));
+        }
+    }
     if (st == FDTD_OK)
         st = cu(cudaStreamSynchronize(s->stream));
     if (st != FDTD_OK) {
@@ -390,6 +409,8 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     *out = s;
     return FDTD_OK;
 }
+
+double fdtd_solver_memless_fraction(const fdtd_solver *s) { return s ? s->memless_fraction : 0.0; }
 
 int fdtd_solver_destroy(fdtd_solver *s)
 {
@@ -418,6 +439,7 @@ int fdtd_solver_destroy(fdtd_solver *s)
     if (s->stream) cudaStreamDestroy(s->stream);
     if (s->copy_stream) cudaStreamDestroy(s->copy_stream);
     if (s->d_block) cudaFree(s->d_block);
+    if (s->d_memless) cudaFree(s->d_memless);
     fdtd_plan_destroy(s->plan);
     delete s;
     return FDTD_OK;

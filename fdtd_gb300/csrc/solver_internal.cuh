@@ -35,6 +35,9 @@ struct fdtd_solver {
     float *d[2][3] = {};
     uint8_t *mat = nullptr;
     uint32_t *rexp = nullptr;  // FDTD_KERNEL_COMPACT_R16: scale words (d[0] holds the FP16 residuals)
+    unsigned long long *d_memless = nullptr;  // compact forms: the strip kernel's memoryless-plane masks
+    double memless_fraction = 0.0;            // share of the cell-updates on such planes
+    int memless_rows = 0;                     // tile rows of those masks
     int *counter = nullptr;
     int steps = 0;
     std::map<std::pair<int, int>, cudaGraphExec_t> graphs;  // (parity, length) -> exec

@@ -26,6 +26,10 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
+#include <cstring>
+
+#include "cell_math.cuh"
 #include "native.cuh"
 #include "per_device.h"
 #include "tma_util.cuh"
@@ -151,41 +155,6 @@ __device__ __forceinline__ bool unit_has_source(const NativeConsts &c, int x0, i
 __device__ __forceinline__ size_t r16_word(const NativeConsts &c, int z, int bx, int y)
 {
     return ((size_t)z * r16_segments(c.nx) + bx) * r16_rows(c.ny) + y;
-}
-
-// The scale 2^(b - 127) of a segment's word w (b in its low byte; w = 0
-// gives 0).
-__device__ __forceinline__ float r16_scale(uint32_t w) { return __uint_as_float(w << 23); }
-
-// The residual of a cell from its stored FP16 bits h and its segment's
-// scale (exact while the product stays in FP32's normal range: an FP16
-// value has 11 significant bits and the scale is a power of two).
-__device__ __forceinline__ float r16_decode(unsigned short h, float scale)
-{
-    float f;
-    asm("cvt.f32.f16 %0, %1;" : "=f"(f) : "h"(h));
-    return f * scale;
-}
-
-// Warp-collective (every lane of the warp calls it; one warp is one row
-// segment): b = e - 14, at least 1, for the largest |r0|, |r1|, |r2| of the
-// segment with biased exponent e; returns b and sets each hk to the FP16
-// bits of rk 2^(127-b) rounded to nearest even.  The scaling by a power of
-// two is exact and puts the segment's largest value in [2^14, 2^15), below
-// the FP16 maximum; every value above 2^-29 of it keeps FP16's 11
-// significant bits, so the three components share one scale.  Lanes
-// outside the grid pass zeros.
-__device__ __forceinline__ uint32_t r16_encode(float r0, float r1, float r2, unsigned short &h0, unsigned short &h1,
-                                               unsigned short &h2)
-{
-    const float a = fmaxf(fmaxf(fabsf(r0), fabsf(r1)), fabsf(r2));
-    const unsigned m = __reduce_max_sync(0xffffffffu, __float_as_uint(a));
-    const uint32_t b = (uint32_t)max((int)(m >> 23) - 14, 1);
-    const float mult = __uint_as_float((254u - b) << 23);
-    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h0) : "f"(r0 * mult));
-    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h1) : "f"(r1 * mult));
-    asm("cvt.rn.f16.f32 %0, %1;" : "=h"(h2) : "f"(r2 * mult));
-    return b;
 }
 
 // One work unit: the column tile (bx, by) and z chunk bz of one solve.  The
@@ -325,11 +294,11 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
             hyn = ha(1, r, cc);
             hzn = ha(2, r, cc);
             if (x >= 1 && x < nx - 1 && y < ny - 1 && zlo)
-                hxn = hxn - ky * (ea(2, r + 1, cc) - ez_) + ky * (eb(1, r, cc) - ey_);
+                hxn = cm_h(hxn, ky, ea(2, r + 1, cc), ez_, ky, eb(1, r, cc), ey_);
             if (x < nx - 1 && y >= 1 && y < ny - 1 && zlo)
-                hyn = hyn - kz * (eb(0, r, cc) - ex_) + kx * (ea(2, r, cc + 1) - ez_);
+                hyn = cm_h(hyn, kz, eb(0, r, cc), ex_, kx, ea(2, r, cc + 1), ez_);
             if (x < nx - 1 && y < ny - 1 && zmid)
-                hzn = hzn - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+                hzn = cm_h(hzn, kx, ea(1, r, cc + 1), ey_, ky, ea(0, r + 1, cc), ex_);
         }
         if (z < zc0) {  // chunk prologue: only this column's H at zc0 - 1 is needed
             hxm = hxn;
@@ -350,11 +319,11 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     const int xh = x0 - 1;
                     float v = ha(1, r, cc);
                     if (yy >= 1 && yy < ny - 1 && zlo)
-                        v = v - kz * (eb(0, r, cc) - ex_) + kx * (ea(2, r, cc + 1) - ez_);
+                        v = cm_h(v, kz, eb(0, r, cc), ex_, kx, ea(2, r, cc + 1), ez_);
                     hnr(1, row + 1, 0) = v;
                     v = ha(2, r, cc);
                     if (xh < nx - 1 && yy < ny - 1 && zmid)
-                        v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+                        v = cm_h(v, kx, ea(1, r, cc + 1), ey_, ky, ea(0, r + 1, cc), ex_);
                     hnr(2, row + 1, 0) = v;
                 }
             }
@@ -365,11 +334,11 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 const float ex_ = ea(0, r, cc), ey_ = ea(1, r, cc), ez_ = ea(2, r, cc);
                 float v = ha(0, r, cc);
                 if (x >= 1 && x < nx - 1 && zlo)
-                    v = v - ky * (ea(2, r + 1, cc) - ez_) + ky * (eb(1, r, cc) - ey_);
+                    v = cm_h(v, ky, ea(2, r + 1, cc), ez_, ky, eb(1, r, cc), ey_);
                 hnr(0, 0, tx + 1) = v;
                 v = ha(2, r, cc);
                 if (x < nx - 1 && zmid)
-                    v = v - kx * (ea(1, r, cc + 1) - ey_) + ky * (ea(0, r + 1, cc) - ex_);
+                    v = cm_h(v, kx, ea(1, r, cc + 1), ey_, ky, ea(0, r + 1, cc), ex_);
                 hnr(2, 0, tx + 1) = v;
             }
             if (TMA) {
@@ -432,9 +401,9 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 const bool dz_on = xi && yi && zlo;
                 float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
                 if (dx_on)
-                    g0 = tcy * (hzn - hnr(2, ty, tx + 1)) - tcz * (hyn - hym);
+                    g0 = cm_dinc(tcy, hzn, hnr(2, ty, tx + 1), tcz, hyn, hym);
                 if (dy_on)
-                    g1 = tcz * (hxn - hxm) - tcx * (hzn - hnr(2, ty + 1, tx));
+                    g1 = cm_dinc(tcz, hxn, hxm, tcx, hzn, hnr(2, ty + 1, tx));
                 // the per-cell test over the source list, in units that hold a
                 // source only, measured faster than the column mask in this form
                 // (which needs three more registers of the 48)
@@ -443,9 +412,9 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                     for (int s = 0; s < c.nsources; s++)
                         src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
                 if (dz_on || src) {
-                    g2 = tcx * (hyn - hnr(1, ty + 1, tx)) - tcy * (hxn - hnr(0, ty, tx + 1));
+                    g2 = cm_dinc(tcx, hyn, hnr(1, ty + 1, tx), tcy, hxn, hnr(0, ty, tx + 1));
                     if (src)
-                        g2 = g2 - jz_now;
+                        g2 = __fsub_rn(g2, jz_now);
                 }
 
                 // ---- E^{n+1} = c (d E^n + (2 dt + 2 tau) dD + R^n),  R^{n+1} = -a E^n - 2 tau dD
@@ -453,36 +422,36 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 const bool eyz_on = x >= 1 && z >= 1;
                 if (ex_on || eyz_on) {
                     const DebyeCoef kc = coef[min((int)cls, cls_max)];
-                    const float k12 = kc.two_dt + kc.two_tau;
+                    const float k12 = cm_k12(kc);
                     const int r = ty + 1, cc = tx + 4;
                     if constexpr (R16) {  // R^n = rho - a E^n
-                        const float sc = r16_scale(w);
-                        r0 = fmaf(-kc.a, ea(0, r, cc), r16_decode(q0, sc));
-                        r1 = fmaf(-kc.a, ea(1, r, cc), r16_decode(q1, sc));
-                        r2 = fmaf(-kc.a, ea(2, r, cc), r16_decode(q2, sc));
+                        const float sc = cm_r16_scale(w);
+                        r0 = cm_r16_r(q0, sc, kc.a, ea(0, r, cc));
+                        r1 = cm_r16_r(q1, sc, kc.a, ea(1, r, cc));
+                        r2 = cm_r16_r(q2, sc, kc.a, ea(2, r, cc));
                     }
                     if (ex_on) {
                         const float e = ea(0, r, cc);
-                        const float en = kc.c * (kc.d * e + k12 * g0 + r0);
-                        const float rn = -kc.a * e - kc.two_tau * g0;
+                        const float en = cm_e_next(kc, k12, e, g0, r0);
+                        const float rn = cm_r_next(kc, e, g0);
                         c.e_prev[0][i] = en;
                         if constexpr (R16) {
-                            rho0 = fmaf(kc.a, en, rn);
+                            rho0 = cm_r16_rho(kc.a, en, rn);
                         } else {
                             c.d_prev[0][i] = rn;
                         }
                     }
                     if (eyz_on) {
                         const float e1 = ea(1, r, cc), e2 = ea(2, r, cc);
-                        ey_new = kc.c * (kc.d * e1 + k12 * g1 + r1);
-                        ez_new = kc.c * (kc.d * e2 + k12 * g2 + r2);
+                        ey_new = cm_e_next(kc, k12, e1, g1, r1);
+                        ez_new = cm_e_next(kc, k12, e2, g2, r2);
                         c.e_prev[1][i] = ey_new;
-                        const float rn1 = -kc.a * e1 - kc.two_tau * g1;
+                        const float rn1 = cm_r_next(kc, e1, g1);
                         c.e_prev[2][i] = ez_new;
-                        const float rn2 = -kc.a * e2 - kc.two_tau * g2;
+                        const float rn2 = cm_r_next(kc, e2, g2);
                         if constexpr (R16) {
-                            rho1 = fmaf(kc.a, ey_new, rn1);
-                            rho2 = fmaf(kc.a, ez_new, rn2);
+                            rho1 = cm_r16_rho(kc.a, ey_new, rn1);
+                            rho2 = cm_r16_rho(kc.a, ez_new, rn2);
                         } else {
                             c.d_prev[1][i] = rn1;
                             c.d_prev[2][i] = rn2;
@@ -496,7 +465,7 @@ __device__ __forceinline__ bool fused_unit(const NativeConsts &c, const FusedMap
                 // store 0)
                 if (y < ny) {  // uniform over the warp: one warp is one row
                     unsigned short h0, h1, h2;
-                    const uint32_t b = r16_encode(rho0, rho1, rho2, h0, h1, h2);
+                    const uint32_t b = cm_r16_encode(rho0, rho1, rho2, h0, h1, h2);
                     if (x < nx) {
                         reinterpret_cast<unsigned short *>(c.d_prev[0])[i] = h0;
                         reinterpret_cast<unsigned short *>(c.d_prev[1])[i] = h1;
@@ -1003,10 +972,22 @@ int launch_h_de_fused(const NativeConsts &c, cudaStream_t s)
     return launch_fused_impl<false, false>(a, maps, s);
 }
 
+// The compact forms run the strip kernel (step_strip.cu) wherever its TMA
+// loads and stores can address the arrays, else the z-marching kernel here;
+// FDTD_COMPACT_STEP=zmarch in the environment selects the z-marching kernel
+// everywhere (both give the same bits; used to cross-check them).
+static bool strip_selected(const NativeConsts &c, bool r16)
+{
+    const char *v = std::getenv("FDTD_COMPACT_STEP");
+    return !(v && std::strcmp(v, "zmarch") == 0) && strip_usable(c, r16);
+}
+
 int launch_h_e_compact(const NativeConsts &c, cudaStream_t s)
 {
     if (c.d_cur[0] != c.d_prev[0] || c.d_cur[1] != c.d_prev[1] || c.d_cur[2] != c.d_prev[2])
         return FDTD_ERR_INVALID;  // R is updated in place
+    if (strip_selected(c, false))
+        return launch_strip_compact(c, s);
     static_assert(FDTD_COMPACT_ZCHUNK >= 4, "z chunks hold at least four planes");
     FusedArgs a;
     a.c = c;
@@ -1021,6 +1002,8 @@ int launch_h_e_compact16(const NativeConsts &c, cudaStream_t s)
 {
     if (c.d_cur[0] != c.d_prev[0] || c.d_cur[1] != c.d_prev[1] || c.d_cur[2] != c.d_prev[2] || !c.r_exp)
         return FDTD_ERR_INVALID;  // R and its scale words are updated in place
+    if (strip_selected(c, true))
+        return launch_strip_compact16(c, s);
     FusedArgs a;
     a.c = c;
     a.zchunk = compact_zchunk(c.nz);

@@ -37,7 +37,8 @@ enum fdtd_status_code {
     FDTD_ERR_NO_SYMBOLS = 10004,  /* a compat launcher ran before fdtd_copy_symbols on this device */
     FDTD_ERR_NOMEM = 10005,       /* a host allocation failed */
     FDTD_ERR_STATE = 10006,       /* call not valid in the object's current state */
-    FDTD_ERR_DEVICE_TIMEOUT = 10007 /* a kernel's bounded wait gave up; its results are invalid */
+    FDTD_ERR_DEVICE_TIMEOUT = 10007, /* a kernel's bounded wait gave up; its results are invalid */
+    FDTD_ERR_BUSY = 10008         /* the queued GPU work a ticket marks has not finished yet */
 };
 
 /* Human-readable text for any status this library returns. */
@@ -333,6 +334,12 @@ typedef struct fdtd_solver_config {
 
 int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out);
 int fdtd_solver_destroy(fdtd_solver *s);
+/* Compact forms: the share of a step's cell-updates that lie on tile-planes
+ * (32 x 8 cells of one z plane) whose classes all have tau = 0.  There the
+ * recursion variable R stays +0, and the step kernel neither reads nor writes
+ * it (no reference counterpart: the reference stores its Debye history for
+ * every cell).  0 for the D form. */
+double fdtd_solver_memless_fraction(const fdtd_solver *s);
 
 /* Enqueue nsteps steps on the solver's stream (asynchronous). */
 int fdtd_solver_run(fdtd_solver *s, int nsteps);
@@ -440,6 +447,14 @@ const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k);
  * counter advance, replayed as a CUDA graph.  A solve stops at its own step
  * target; adding or removing a solve rebuilds the launch.  Results of a solve
  * are identical whether it runs alone or with others.
+ *
+ * A running batch is never drained for bookkeeping: fdtd_batch_add uploads
+ * the new solve on a side stream (the batch stream waits for it before the
+ * solve's first step), fdtd_batch_remove frees in stream order behind the
+ * steps already queued, and fdtd_batch_read_async / fdtd_batch_mark queue a
+ * copy or a marker and return a ticket that fdtd_batch_ticket polls.  Device
+ * memory of the solves comes from the batch's own stream-ordered pool, which
+ * keeps freed memory for later solves until the batch is destroyed.
  * ---------------------------------------------------------------------- */
 
 typedef struct fdtd_batch fdtd_batch;
@@ -456,8 +471,12 @@ size_t fdtd_batch_solve_bytes(int nx, int ny, int nz);
 /* The same for a solve of this batch's form. */
 size_t fdtd_batch_need_bytes(const fdtd_batch *b, int nx, int ny, int nz);
 /* Adds a solve (cfg->kernel and cfg->device are ignored: the batch's form and
- * device apply) that will run `steps` steps; *id receives its handle. */
+ * device apply) that will run `steps` steps; *id receives its handle.  Waits
+ * only for the solve's own uploads, not for queued steps; it joins at the
+ * next fdtd_batch_run. */
 int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int *id);
+/* Removes a solve; its memory is released in stream order after the steps
+ * and reads already queued (no wait). */
 int fdtd_batch_remove(fdtd_batch *b, int id);
 /* Enqueues nsteps batched steps (asynchronous). */
 int fdtd_batch_run(fdtd_batch *b, int nsteps);
@@ -476,9 +495,34 @@ int fdtd_batch_steps(fdtd_batch *b, int id);
 /* Copies planes [z0, z0 + nplanes) (nplanes 0 = all) of one field of one
  * solve into host memory, nx*ny*nplanes floats. */
 int fdtd_batch_get_field(fdtd_batch *b, int id, int field, int z0, int nplanes, float *host_out);
+/* Queues a copy of planes [z0, z0 + nplanes) (nplanes 0 = all) of one field
+ * of one solve, as they will be after the steps queued so far, into host
+ * memory (nx*ny*nplanes floats; page-locked memory, e.g. fdtd_host_alloc,
+ * keeps the copy asynchronous), without waiting.  *ticket: poll it with
+ * fdtd_batch_ticket; host_out holds the planes once it reports done.  The
+ * reference's snapshot path copies into pinned buffers the same way
+ * (fdtd.cu:134-136). */
+int fdtd_batch_read_async(fdtd_batch *b, int id, int field, int z0, int nplanes, float *host_out,
+                          long long *ticket);
+/* A ticket for the point after everything queued so far. */
+int fdtd_batch_mark(fdtd_batch *b, long long *ticket);
+/* FDTD_OK once the ticket's work has finished (the ticket is then spent),
+ * FDTD_ERR_BUSY while it has not (wait = 0), or a CUDA error; wait != 0
+ * blocks until it finishes. */
+int fdtd_batch_ticket(fdtd_batch *b, long long ticket, int wait);
+/* With timing on, every fdtd_batch_run is bracketed by events;
+ * fdtd_batch_busy returns the GPU time of the finished runs and the time from
+ * the first run's start to the last finished run's end (their ratio is the
+ * fraction of time the batch kept the GPU busy). */
+int fdtd_batch_set_timing(fdtd_batch *b, int on);
+int fdtd_batch_busy(fdtd_batch *b, double *busy_ms, double *span_ms);
 size_t fdtd_batch_bytes(const fdtd_batch *b);
 int fdtd_batch_size(const fdtd_batch *b);
 fdtd_stream_t fdtd_batch_stream(const fdtd_batch *b);
+
+/* Page-locked host memory for asynchronous copies (cudaHostAlloc / cudaFreeHost). */
+int fdtd_host_alloc(size_t bytes, void **out);
+int fdtd_host_free(void *p);
 
 #ifdef __cplusplus
 }
