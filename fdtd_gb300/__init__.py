@@ -174,6 +174,7 @@ def lib() -> C.CDLL:
         _sig(L, "fdtd_batch_run", _I, _V, _I)
         _sig(L, "fdtd_batch_synchronize", _I, _V)
         _sig(L, "fdtd_batch_autotune", _I, _V, _I, C.POINTER(_I))
+        _sig(L, "fdtd_batch_tuning", _I, _V, C.POINTER(_I), C.POINTER(_I), C.POINTER(_I))
         _sig(L, "fdtd_batch_steps", _I, _V, _I)
         _sig(L, "fdtd_batch_get_field", _I, _V, _I, _I, _I, _I, _P)
         _sig(L, "fdtd_batch_bytes", C.c_size_t, _V)
@@ -515,6 +516,13 @@ class Batch:
         chosen = C.c_int(0)
         check(lib().fdtd_batch_autotune(self.handle, steps_per_trial, C.byref(chosen)), "fdtd_batch_autotune")
         return chosen.value
+
+    def tuning(self) -> dict:
+        """The launch shape in use: z-chunk limit (0: default), tile rows and
+        the strip kernel's shape (-1: D form)."""
+        z, r, sh = C.c_int(), C.c_int(), C.c_int()
+        check(lib().fdtd_batch_tuning(self.handle, C.byref(z), C.byref(r), C.byref(sh)), "fdtd_batch_tuning")
+        return {"z_chunk_limit": z.value, "tile_rows": r.value, "strip_shape": sh.value}
 
     def steps(self, sid: int) -> int:
         return lib().fdtd_batch_steps(self.handle, sid)

@@ -23,7 +23,7 @@ CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["compat.cu", "native.cu", "step_fused.cu", "step_strip.cu", "step_static.cu", "solver.cu", "monitor.cu", "batch.cu", "cuda_util.cu"]
+CU_SOURCES = ["compat.cu", "native.cu", "step_fused.cu", "step_strip.cu", "batch_strip.cu", "step_static.cu", "solver.cu", "monitor.cu", "batch.cu", "cuda_util.cu"]
 CPP_SOURCES = ["host_io.cpp"]
 HEADERS = ["fdtd_internal.h", "device_common.cuh", "native.cuh", "solver_internal.cuh", "tma_util.cuh", "per_device.h", "cell_math.cuh", "strip_unit.cuh"]
 

@@ -28,8 +28,13 @@
 #include <vector>
 
 #include "native.cuh"
+#include "strip_unit.cuh"
 
 using namespace fdtd;
+
+namespace {
+constexpr int STRIP_SHAPE_COUNT = strip::STRIP_SHAPES;
+}
 
 namespace {
 
@@ -51,6 +56,7 @@ struct BatchSolve {
     int *counter = nullptr;
     int host_steps = 0;              // steps queued for this solve so far (its counter once they ran)
     cudaEvent_t ready = nullptr;     // its uploads on the side stream; waited for before its first step
+    std::vector<unsigned char> memless8;  // compact forms: tile-planes (32 x 8) without Debye memory
 };
 
 size_t padded_pitch(int nx) { return ((size_t)nx + 15) & ~size_t(15); }
@@ -110,6 +116,10 @@ struct fdtd_batch {
     std::map<int, cudaGraphExec_t> graphs;  // steps per graph -> exec
     size_t bytes = 0;
     int zchunk_max = 0;  // largest z chunk (fdtd_batch_autotune); 0: the form's default
+    int strip_shape = 1;  // compact forms: strip kernel shape, -1 the z-marching kernel (fdtd_batch_autotune)
+    bool strip = false;   // the current launch runs the strip kernel
+    unsigned long long *d_memless = nullptr;  // per unit: planes whose tile has no Debye memory
+    size_t memless_cap = 0;
 };
 
 namespace {
@@ -226,18 +236,29 @@ int rebuild(fdtd_batch *b)
     std::vector<BatchDesc> descs(b->solves.size());
     std::vector<BatchMurBlock> mur;
     int units = 0;
-    const int ty = fused_tile_height();
+    // compact forms run the strip kernel when every solve's arrays are
+    // TMA-addressable for it (and the autotuner did not choose the
+    // z-marching kernel: shape -1), else the z-marching kernel
+    bool strip = b->compact && b->strip_shape >= 0;
+    for (auto *v : b->solves)
+        if (strip) {
+            NativeConsts c = solve_consts(v, 0, b->d_work + BATCH_ERR_WORD);
+            strip = strip_usable(c, b->r16);
+        }
+    const int ty = strip ? strip_shape_rows(b->strip_shape) : fused_tile_height();
     for (size_t i = 0; i < b->solves.size(); i++) {
         BatchSolve *v = b->solves[i];
         BatchDesc &d = descs[i];
         std::memset(&d, 0, sizeof d);
         for (int par = 0; par < 2; par++) {
             d.c[par] = solve_consts(v, par, b->d_work + BATCH_ERR_WORD);
-            if (!encode_step_maps(d.c[par], b->compact, &d.maps[par], b->r16))
+            if (strip ? !strip::encode_strip_maps(d.c[par], b->r16, ty, &d.smaps[par])
+                      : !encode_step_maps(d.c[par], b->compact, &d.maps[par], b->r16))
                 return FDTD_ERR_INVALID;
         }
         d.zchunk = b->zchunk_max > 0 ? zchunk_limited(v->nz, b->zchunk_max)
-                                     : (b->compact ? compact_zchunk(v->nz) : fused_zchunk(v->nz));
+                                     : (strip ? strip_zchunk(v->nz)
+                                              : (b->compact ? compact_zchunk(v->nz) : fused_zchunk(v->nz)));
         d.tiles_x = (v->nx + 31) / 32;
         d.tiles_y = (v->ny + ty - 1) / ty;
         d.chunks = (v->nz + d.zchunk - 1) / d.zchunk;
@@ -278,18 +299,42 @@ int rebuild(fdtd_batch *b)
         st = pool_alloc(b, reinterpret_cast<void **>(&b->d_mur), sizeof(BatchMurBlock) * cap, b->stream);
         b->mur_cap = st == FDTD_OK ? cap : 0;
     }
+    // strip kernel: per unit, the planes whose tile holds no Debye memory
+    std::vector<unsigned long long> masks;
+    if (strip) {
+        masks.assign((size_t)units, 0ull);
+        for (size_t i = 0; i < b->solves.size(); i++) {
+            const BatchSolve *v = b->solves[i];
+            strip_unit_masks(v->memless8, v->nx, v->ny, v->nz, ty, descs[i].zchunk, masks.data() + descs[i].unit_begin);
+        }
+        if (st == FDTD_OK && masks.size() > b->memless_cap) {
+            if (b->d_memless)
+                cudaFreeAsync(b->d_memless, b->stream);
+            b->d_memless = nullptr;
+            const size_t cap = std::max(masks.size() * 2, size_t(1024));
+            st = pool_alloc(b, reinterpret_cast<void **>(&b->d_memless), sizeof(unsigned long long) * cap, b->stream);
+            b->memless_cap = st == FDTD_OK ? cap : 0;
+        }
+    }
     if (st == FDTD_OK && !descs.empty())
         st = staged_upload(b, b->d_descs, descs.data(), sizeof(BatchDesc) * descs.size());
     if (st == FDTD_OK && !mur.empty())
         st = staged_upload(b, b->d_mur, mur.data(), sizeof(BatchMurBlock) * mur.size());
+    if (st == FDTD_OK && !masks.empty())
+        st = staged_upload(b, b->d_memless, masks.data(), sizeof(unsigned long long) * masks.size());
     if (st != FDTD_OK)
         return st;
     int max_classes = 1;
     for (auto *v : b->solves)
         max_classes = std::max(max_classes, v->plan->nclasses);
-    b->launch = BatchLaunch{b->d_descs, (int)descs.size(), units, b->d_work, b->d_mur, (int)mur.size(),
-                            batch_persistent_ctas(b->compact, max_classes, b->r16), b->compact ? 1 : 0, max_classes,
-                            b->r16 ? 1 : 0};
+    const int ctas = strip ? batch_strip_ctas(b->r16, b->strip_shape, max_classes)
+                           : batch_persistent_ctas(b->compact, max_classes, b->r16);
+    if (ctas < 1)
+        return FDTD_ERR_INVALID;
+    b->launch = BatchLaunch{b->d_descs, (int)descs.size(), units, b->d_work, b->d_mur, (int)mur.size(), ctas,
+                            b->compact ? 1 : 0, max_classes, b->r16 ? 1 : 0, strip ? 1 : 0, b->strip_shape,
+                            strip ? b->d_memless : nullptr};
+    b->strip = strip;
     drop_graphs(b);
     b->dirty = false;
     return FDTD_OK;
@@ -428,6 +473,8 @@ int fdtd_batch_destroy(fdtd_batch *b)
         cudaFreeAsync(b->d_descs, s);
     if (b->d_mur)
         cudaFreeAsync(b->d_mur, s);
+    if (b->d_memless)
+        cudaFreeAsync(b->d_memless, s);
     if (s)
         cudaStreamSynchronize(s);
     cudaFree(b->d_work);
@@ -529,6 +576,8 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         free_solve(v, b->side);
         return st;
     }
+    if (b->compact)
+        v->memless8 = strip_plane_flags(cfg->material, p->nx, p->ny, p->nz, p->nx, cfg->specs, cfg->nclasses);
     v->bytes = total + plan_bytes(p->nx, p->ny, p->nz);
     v->id = b->next_id++;
     b->solves.push_back(v);
@@ -606,20 +655,26 @@ int fdtd_batch_autotune(fdtd_batch *b, int steps_per_trial, int *chosen)
     int st = cu(cudaSetDevice(b->device));
     if (st != FDTD_OK)
         return st;
-    // D form: at most 64 planes (the per-thread source-plane mask covers 66)
-    static const int compact_cands[] = {8, 12, 16, 24, 32, 48, 64};
+    // D form: at most 64 planes (the per-thread source-plane mask covers 66);
+    // compact forms: every strip tile shape with each chunk limit (the
+    // z-marching kernel, where the strip kernel cannot run, takes shape 0's
+    // trials)
+    static const int compact_cands[] = {8, 16, 32, 64};
     static const int dform_cands[] = {16, 24, 32, 48, 64};
-    const int *cands = b->compact ? compact_cands : dform_cands;
-    const int ncand = b->compact ? 7 : 5;
+    const int nz_cand = b->compact ? 4 : 5;
+    const int nshape = b->compact ? STRIP_SHAPE_COUNT + 1 : 1;  // strip shapes, then the z-marching kernel
+    const int ncand = nz_cand * nshape;
     const int trial = (steps_per_trial + 7) / 8 * 8;  // whole 8-step graphs only
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     st = cu(cudaEventCreate(&e0));
     if (st == FDTD_OK)
         st = cu(cudaEventCreate(&e1));
     double best_cost = 0.0;
-    int best = 0;
+    int best = 0, best_shape = b->strip_shape;
     for (int k = 0; k < ncand && st == FDTD_OK && !b->solves.empty(); k++) {
-        b->zchunk_max = cands[k];
+        const int zc = b->compact ? compact_cands[k % nz_cand] : dform_cands[k % nz_cand];
+        b->zchunk_max = zc;
+        b->strip_shape = k / nz_cand < STRIP_SHAPE_COUNT ? k / nz_cand : -1;
         b->dirty = true;
         st = fdtd_batch_run(b, 8);  // rebuild and graph capture, untimed
         double c0 = 0.0, c1 = 0.0;
@@ -640,10 +695,12 @@ int fdtd_batch_autotune(fdtd_batch *b, int steps_per_trial, int *chosen)
             const double cost = ms / (c1 - c0);
             if (best == 0 || cost < best_cost) {
                 best_cost = cost;
-                best = cands[k];
+                best = zc;
+                best_shape = b->strip_shape;
             }
         }
     }
+    b->strip_shape = best_shape;
     if (e0)
         cudaEventDestroy(e0);
     if (e1)
@@ -816,6 +873,19 @@ int fdtd_batch_get_field(fdtd_batch *b, int id, int field, int z0, int nplanes, 
     src += (size_t)z0 * v->pitch * v->ny;
     return cu(cudaMemcpy2D(host_out, sizeof(float) * v->nx, src, sizeof(float) * v->pitch, sizeof(float) * v->nx,
                            (size_t)v->ny * nplanes, cudaMemcpyDeviceToHost));
+}
+
+int fdtd_batch_tuning(const fdtd_batch *b, int *zchunk_max, int *tile_rows, int *strip_kernel)
+{
+    if (!b)
+        return FDTD_ERR_INVALID;
+    if (zchunk_max)
+        *zchunk_max = b->zchunk_max;
+    if (tile_rows)
+        *tile_rows = b->compact && b->strip_shape >= 0 ? strip_shape_rows(b->strip_shape) : fused_tile_height();
+    if (strip_kernel)
+        *strip_kernel = b->compact ? b->strip_shape : -1;
+    return FDTD_OK;
 }
 
 size_t fdtd_batch_bytes(const fdtd_batch *b) { return b ? b->bytes : 0; }

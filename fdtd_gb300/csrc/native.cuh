@@ -140,12 +140,23 @@ struct FusedMaps {
     CUtensorMap m[16];
 };
 
+// Tensor maps of one strip-kernel launch (step_strip.cu, strip_unit.cuh):
+// E^n (0-2), H^{n-1/2} (3-5), R or its FP16 residuals (6-8, loaded and
+// stored in place), classes (9), scale words (10, 16-bit R), H^{n+1/2}
+// (11-13), E^{n+1} (14-16).
+struct StripMaps {
+    CUtensorMap m[17];
+};
+static_assert(sizeof(StripMaps) % 64 == 0, "tensor maps stay 64-byte aligned in arrays");
+
 // One solve of a batch as the batched kernels see it (device memory).  The
-// solve's completed-step count n selects c[n & 1] / maps[n & 1]; units
-// [unit_begin, unit_begin + unit_count) are its (tile x, tile y, z chunk)
-// work items; it is skipped once n reaches steps_target.
+// solve's completed-step count n selects c[n & 1] / maps[n & 1] (smaps in a
+// batch run by the strip kernel); units [unit_begin, unit_begin +
+// unit_count) are its (tile x, tile y, z chunk) work items; it is skipped
+// once n reaches steps_target.
 struct alignas(64) BatchDesc {
     FusedMaps maps[2];
+    StripMaps smaps[2];
     NativeConsts c[2];
     int zchunk, tiles_x, tiles_y, chunks;
     int unit_begin, unit_count;
@@ -172,6 +183,9 @@ struct BatchLaunch {
     int compact;      // the batch's solves keep the compact state (d_cur == d_prev == R)
     int max_classes;  // largest class count of the batch's solves (shared-memory table)
     int r16;          // the compact state holds R in 16 bits (compact is set too)
+    int strip;        // compact forms: run by the strip kernel of shape strip_shape
+    int strip_shape;
+    const unsigned long long *memless;  // strip kernel: memoryless-plane mask per unit (may be null)
 };
 
 // Tensor maps of a single-pass launch over c's buffers (false: not encodable).
@@ -184,6 +198,10 @@ int zchunk_limited(int nz, int max_planes);  // nz in equal chunks of at most ma
 // One batched step: fused kernel over all units, Mur faces, step counters.
 int launch_batch_step(const BatchLaunch &b, cudaStream_t s);
 int batch_persistent_ctas(bool compact, int nclasses, bool r16 = false);
+// The batch's persistent strip kernel (batch_strip.cu): its launch and the
+// CTAs that fill the device at the given shape and class count.
+int launch_batch_strip(const BatchLaunch &b, cudaStream_t s);
+int batch_strip_ctas(bool r16, int shape, int nclasses);
 
 // The compact forms' step kernel with TMA loads and stores over column strips
 // (step_strip.cu); usable when every array is TMA-addressable (rows of a

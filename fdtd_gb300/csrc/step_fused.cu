@@ -934,6 +934,12 @@ int launch_batch_step(const BatchLaunch &b, cudaStream_t s)
 {
     if (b.max_classes < 1 || b.max_classes > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
+    cudaError_t e = cudaSuccess;
+    if (b.strip) {
+        const int st = launch_batch_strip(b, s);
+        if (st != FDTD_OK)
+            return st;
+    } else {
     const int oi = b.r16 ? batch_opt_in<true, true>() : (b.compact ? batch_opt_in<true>() : batch_opt_in<false>());
     if (oi != FDTD_OK)
         return oi;
@@ -949,7 +955,8 @@ int launch_batch_step(const BatchLaunch &b, cudaStream_t s)
         batch_step_kernel<TY_SEL, S_SEL, false>
             <<<b.persistent_ctas, dim3(FTX, TY_SEL), batch_smem<false>(b.max_classes), s>>>(
                 b.descs, b.nsolves, b.total_units, b.work_counter);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
+    }
     if (e == cudaSuccess && b.nmur_blocks > 0) {
         batch_mur_kernel<<<b.nmur_blocks, 256, 0, s>>>(b.descs, b.mur_blocks);
         e = cudaGetLastError();

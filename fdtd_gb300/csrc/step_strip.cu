@@ -42,29 +42,16 @@ __global__ void __launch_bounds__(32 * W) strip_step_kernel(const __grid_constan
         stall = atomicExch(c.stall_once, 0) != 0;
     const unsigned long long memless =
         c.memless ? c.memless[((size_t)bz * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x] : 0ull;
-    unsigned og = 0;
-    strip_unit<RY, W, S, R16>(c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, memless, sm, 0u, og, stall);
+    strip_unit<RY, W, S, R16>(c, maps, a.zchunk, blockIdx.x, blockIdx.y, bz, memless, sm, 0u, stall);
     if (threadIdx.x == G::STORE_TID)
         bulk_wait_all();
 }
 
 // ------------------------------------------------------------------ host side
 
-// Strip shapes: (cells per thread in y, warps per CTA).  0-2 use 8-row tiles
-// (the same shared memory per CTA, 4, 8 or 2 warps), 3 uses 16-row tiles.
-template <int SHAPE> struct Shape;
-template <> struct Shape<0> { static constexpr int RY = 2, W = 4; };
-template <> struct Shape<1> { static constexpr int RY = 1, W = 8; };
-template <> struct Shape<2> { static constexpr int RY = 4, W = 2; };
-template <> struct Shape<3> { static constexpr int RY = 4, W = 4; };
-
-#ifndef FDTD_STRIP_STAGES
-#define FDTD_STRIP_STAGES 3
-#endif
 #ifndef FDTD_STRIP_ZCHUNK
 #define FDTD_STRIP_ZCHUNK 16
 #endif
-constexpr int S_SEL = FDTD_STRIP_STAGES;
 static_assert(FDTD_STRIP_ZCHUNK >= 2 && FDTD_STRIP_ZCHUNK <= 64, "a unit's memoryless-plane mask has 64 bits");
 
 template <int SHAPE, bool R16>
@@ -127,7 +114,7 @@ int single_shape(bool r16)
     const char *v = std::getenv("FDTD_STRIP_SHAPE");
     if (v && v[0] >= '0' && v[0] < '0' + STRIP_SHAPES && v[1] == 0)
         return v[0] - '0';
-    return r16 ? 0 : 0;
+    return 1;  // 1 x 8: the fastest on the 512 x 512 x 400 phantom for both forms
 }
 
 }  // namespace
@@ -233,7 +220,7 @@ double strip_unit_masks(const std::vector<unsigned char> &flags, int nx, int ny,
 
 bool strip_usable(const NativeConsts &c, bool r16)
 {
-    strip::StripMaps maps;
+    StripMaps maps;
     return strip::encode_strip_maps(c, r16, 8, &maps);
 }
 

@@ -17,7 +17,7 @@
 //   (E^n with a one-cell halo, H^{n-1/2} with a low x / low y halo, the tile's
 //   R, class bytes and, with 16-bit R, the rows' scale words).  Outputs go
 //   the same way: each thread writes its results into dense shared-memory
-//   tiles (double-buffered), and one thread stores the plane's H^{n+1/2},
+//   tiles, and one thread stores the plane's H^{n+1/2},
 //   E^{n+1}, R^{n+1} (and scale words) with TMA stores.  No thread computes a
 //   global address per cell.
 // * Tiles whose cells, halo included, all lie inside the update ranges of
@@ -64,7 +64,7 @@ struct StripGeo {
     static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 3u * R_BYTES + X_BYTES + M_BYTES;
     static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
     static constexpr unsigned TX_EPI = 3u * E_BYTES;
-    // one set of output tiles (dense 32 x TY): H^{n+1/2}, E^{n+1}, R^{n+1}, scale words
+    // the output tiles (dense 32 x TY): H^{n+1/2}, E^{n+1}, R^{n+1}, scale words
     static constexpr int T_BYTES = SX * TY * 4;
     static constexpr int O_H = 0, O_E = 3 * T_BYTES, O_R = 6 * T_BYTES;
     static constexpr int O_X = O_R + 3 * pad128(R_BYTES);
@@ -75,18 +75,29 @@ struct StripGeo {
     static constexpr int XC = 2 * TY * (SX + 1), XR = 2 * W * SX;
 };
 
+// Strip shapes: (cells per thread in y, warps per CTA).  0-2 use 8-row tiles
+// (the same shared memory per CTA, 4, 8 or 2 warps), 3 uses 16-row tiles.
 constexpr int STRIP_SHAPES = 4;
+template <int SHAPE> struct Shape;
+template <> struct Shape<0> { static constexpr int RY = 2, W = 4; };
+template <> struct Shape<1> { static constexpr int RY = 1, W = 8; };
+template <> struct Shape<2> { static constexpr int RY = 4, W = 2; };
+template <> struct Shape<3> { static constexpr int RY = 4, W = 4; };
+
+#ifndef FDTD_STRIP_STAGES
+#define FDTD_STRIP_STAGES 3
+#endif
+constexpr int S_SEL = FDTD_STRIP_STAGES;  // ring stages
 
 // Tensor maps of one strip launch over c's buffers for ty-row tiles (false:
 // not TMA-addressable).
-struct StripMaps;
 bool encode_strip_maps(const NativeConsts &c, bool r16, int ty, StripMaps *maps);
 
 template <int RY, int W, int S, bool R16>
 constexpr int strip_smem_bytes(int nclasses)
 {
     using G = StripGeo<RY, W, R16>;
-    return 128 + S * G::STAGE + 2 * G::OUT + 4 * (G::XC + G::XR) + ((S * 8 + 15) & ~15) + nclasses * 32;
+    return 128 + S * G::STAGE + G::OUT + 4 * (G::XC + G::XR) + ((S * 8 + 15) & ~15) + nclasses * 32;
 }
 
 struct StripArgs {
@@ -94,13 +105,7 @@ struct StripArgs {
     int zchunk;
 };
 
-// Tensor maps: E^n (0-2), H^{n-1/2} (3-5), R or its FP16 residuals (6-8,
-// loaded and stored in place), classes (9), scale words (10, 16-bit R),
-// H^{n+1/2} (11-13), E^{n+1} (14-16).
-struct StripMaps {
-    CUtensorMap m[17];
-};
-static_assert(sizeof(StripMaps) % 64 == 0, "tensor maps stay 64-byte aligned in arrays");
+
 
 __device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, uint32_t src, int x, int y, int z)
 {
@@ -158,8 +163,11 @@ __device__ __forceinline__ bool strip_has_source(const NativeConsts &c, int x0, 
     return any;
 }
 
-// A CTA's shared memory: S ring stages, two output sets, the H exchange
-// rows, S barriers, the class table.
+// A CTA's shared memory: S ring stages, the output tiles, the H exchange
+// rows, S barriers, the class table.  The store of a plane's output tiles
+// must have read them before the next plane writes them: the storing thread
+// waits for that before the next plane's first barrier, so the store has a
+// whole H pass to drain.
 struct StripSmem {
     unsigned char *stages, *outs;
     float *hnx, *xrw;
@@ -174,7 +182,7 @@ __device__ __forceinline__ StripSmem strip_smem(unsigned char *smem_raw)
     StripSmem m;
     m.stages = smem_raw + ((128 - (smem_addr(smem_raw) & 127)) & 127);
     m.outs = m.stages + S * G::STAGE;
-    m.hnx = reinterpret_cast<float *>(m.outs + 2 * G::OUT);   // [2][TY][33]
+    m.hnx = reinterpret_cast<float *>(m.outs + G::OUT);       // [2][TY][33]
     m.xrw = m.hnx + G::XC;                                     // [2][W][32]
     m.bars = reinterpret_cast<uint64_t *>(m.xrw + G::XR);
     m.coef = reinterpret_cast<DebyeCoef *>(reinterpret_cast<unsigned char *>(m.bars) + ((S * 8 + 15) & ~15));
@@ -201,15 +209,14 @@ __device__ __forceinline__ void strip_load_coef(const NativeConsts &c, DebyeCoef
 
 // One work unit: column tile (bx, by), z chunk bz of one solve.  The ring's
 // stages and barrier phases continue from earlier units of the same CTA (g0
-// planes staged before), and so do the output sets (og planes stored
-// before; advanced here).  memless: bit j set when plane zc0 + j of the tile
+// planes staged before).  memless: bit j set when plane zc0 + j of the tile
 // holds no Debye memory.  stall (thread 0 only): leave the second plane's
 // copies unissued (test hook).  Returns false when a bounded wait gave up
 // (the error flag is raised; the CTA must stop).
 template <int RY, int W, int S, bool R16>
 __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMaps &maps, int zchunk, int bx, int by,
                                            int bz, unsigned long long memless, const StripSmem &sm, unsigned g0,
-                                           unsigned &og, bool stall)
+                                           bool stall)
 {
     using G = StripGeo<RY, W, R16>;
     constexpr int TY = G::TY;
@@ -374,9 +381,10 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             }
             // the CTA decides here whether a wait gave up (nothing has
             // reached global memory from this plane yet)
-            // the output set this plane writes was stored two planes ago
+            // the output tiles this plane writes were stored one plane ago:
+            // that store has read them by now (checked before the barrier)
             if (tid == G::STORE_TID)
-                bulk_wait_read<1>();
+                bulk_wait_read<0>();
             if (__syncthreads_or(!ok)) {
                 give_up(k);
                 return false;
@@ -384,8 +392,7 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
 
             // ---- D increment, sources, E^{n+1} and R^{n+1} on the strip
             const bool plane_no_r = no_r(z);  // uniform: R is +0 on every cell of the tile-plane
-            unsigned char *O = sm.outs + (og & 1) * G::OUT;
-            og++;
+            unsigned char *O = sm.outs;
             float *OH = reinterpret_cast<float *>(O + G::O_H);
             float *OE = reinterpret_cast<float *>(O + G::O_E);
             const unsigned char *M = stage(k) + G::OFF_M;

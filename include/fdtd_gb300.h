@@ -481,14 +481,24 @@ int fdtd_batch_remove(fdtd_batch *b, int id);
 /* Enqueues nsteps batched steps (asynchronous). */
 int fdtd_batch_run(fdtd_batch *b, int nsteps);
 /* Chooses the z-blocking depth of the batched kernel for the current solves
- * (no counterpart in the reference): times steps_per_trial steps (rounded up
- * to a multiple of 8, after 8 untimed steps) at each candidate largest z
- * chunk (compact form 8-64 planes, D form 16-64) and keeps the one with the
- * least time per cell-update.  The trial steps are real steps of the solves
+ * and, in the compact forms, the strip kernel's tile shape (no counterpart in
+ * the reference): times steps_per_trial steps (rounded up to a multiple of 8,
+ * after 8 untimed steps) at each candidate (compact forms: every strip tile
+ * shape and the z-marching kernel, with largest z chunks of 8, 16, 32, 64
+ * planes; D form 16-64 planes) and
+ * keeps the one with the least time per cell-update.  The trial steps are real steps of the solves
  * (a cell's update does not depend on where chunks meet, so the results are
  * the same bits).  *chosen (optional): the chunk limit kept, 0 if no trial
  * advanced a solve (the form's default stays).  Synchronises. */
 int fdtd_batch_autotune(fdtd_batch *b, int steps_per_trial, int *chosen);
+/* The launch shape in use (no counterpart in the reference): the largest z
+ * chunk (0: the form's default), the rows of the column tiles, and for the
+ * compact forms the strip kernel's shape (0-3: 2 x 4, 1 x 8 and 4 x 2 cells
+ * per thread x warps on 8-row tiles, 4 x 4 on 16-row tiles; -1 for the
+ * z-marching kernel and for the D form).  fdtd_batch_autotune chooses the
+ * compact forms' kernel and shape together with the chunk limit, timing every
+ * pair. */
+int fdtd_batch_tuning(const fdtd_batch *b, int *zchunk_max, int *tile_rows, int *strip_shape);
 int fdtd_batch_synchronize(fdtd_batch *b);
 /* Completed steps of one solve (synchronises; -1 on error). */
 int fdtd_batch_steps(fdtd_batch *b, int id);
