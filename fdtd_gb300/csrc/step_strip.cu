@@ -9,6 +9,9 @@
 #include "strip_unit.cuh"
 
 namespace fdtd {
+
+int strip_zchunk(int nz);
+
 namespace strip {
 namespace {
 
@@ -66,7 +69,7 @@ int launch_shape(const NativeConsts &c, cudaStream_t s)
     a.c = c;
     if (a.c.memless_rows != G::TY)
         a.c.memless = nullptr;  // masks made for another tile height
-    a.zchunk = zchunk_limited(c.nz, FDTD_STRIP_ZCHUNK);
+    a.zchunk = strip_zchunk(c.nz);
     StripMaps maps;
     if (!encode_strip_maps(c, R16, G::TY, &maps))
         return FDTD_ERR_INVALID;
@@ -114,7 +117,9 @@ int single_shape(bool r16)
     const char *v = std::getenv("FDTD_STRIP_SHAPE");
     if (v && v[0] >= '0' && v[0] < '0' + STRIP_SHAPES && v[1] == 0)
         return v[0] - '0';
-    return 1;  // 1 x 8: the fastest on the 512 x 512 x 400 phantom for both forms
+    // measured fastest on the 512 x 512 x 400 phantom: 2 x 4 for 16-bit R,
+    // 1 x 8 for 32-bit R (whose larger stages leave fewer CTAs per SM)
+    return r16 ? 0 : 1;
 }
 
 }  // namespace
@@ -165,7 +170,18 @@ int strip_shape_rows(int shape)
 
 int strip_single_shape(bool r16) { return strip::single_shape(r16); }
 
-int strip_zchunk(int nz) { return zchunk_limited(nz, FDTD_STRIP_ZCHUNK); }
+int strip_zchunk(int nz)
+{
+    // FDTD_STRIP_ZCHUNK in the environment (2-64 planes) overrides the
+    // build's limit; read wherever the launch and the masks are made
+    int limit = FDTD_STRIP_ZCHUNK;
+    if (const char *v = std::getenv("FDTD_STRIP_ZCHUNK")) {
+        const int n = std::atoi(v);
+        if (n >= 2 && n <= 64)
+            limit = n;
+    }
+    return zchunk_limited(nz, limit);
+}
 
 std::vector<unsigned char> strip_plane_flags(const uint8_t *mat, int nx, int ny, int nz, int pitch, const float *specs,
                                              int nclasses)

@@ -140,18 +140,25 @@ def test_compact16_batch_matches_lone_solves_and_oracle(cuda):
 @pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT, fg.KERNEL_COMPACT_R16])
 def test_autotuned_batch_gives_the_same_bits(cuda, kernel):
     """fdtd_batch_autotune times real steps of the solves at each candidate
-    z-chunk limit and keeps the fastest.  A cell's update does not depend on
-    where chunks meet, so every solve still equals the same solve run alone,
+    (compact forms: the four strip tile shapes and the z-marching kernel, each
+    with four z-chunk limits; D form: five z-chunk limits) and keeps the
+    fastest.  A cell's update depends neither on where tiles and chunks meet
+    nor on the kernel, so every solve still equals the same solve run alone,
     bit for bit, and the steps taken while tuning count."""
-    steps = 150  # outlasts the trials (at most 7 candidates x 16 steps)
+    compact = kernel in fg.COMPACT_KERNELS
+    cands, trials = ((8, 16, 32, 64), 20) if compact else ((16, 24, 32, 48, 64), 5)
+    steps = 16 * trials + 80  # outlasts the trials (16 steps each)
     b = fg.Batch(kernel=kernel)
     cases = [_case(k) for k in range(len(CASES))]
     ids = [b.add(Params(c[8]), c[3], c[4], steps, scheme=c[2]) for c in cases]
     chosen = b.autotune(steps_per_trial=8)
-    cands = (8, 12, 16, 24, 32, 48, 64) if kernel in fg.COMPACT_KERNELS else (16, 24, 32, 48, 64)
     assert chosen in cands
+    t = b.tuning()
+    assert t["z_chunk_limit"] == chosen
+    if compact:
+        assert t["strip_shape"] in (-1, 0, 1, 2, 3) and t["tile_rows"] in (8, 16), t
     done = b.steps(ids[0])
-    assert 16 * len(cands) - 8 <= done <= 16 * len(cands), done
+    assert 16 * trials - 8 <= done <= 16 * trials, done
     b.run(steps - done)
     for sid, case in zip(ids, cases):
         dims, _, scheme, codes, specs, sources, consts, jz, raw = case
