@@ -662,7 +662,7 @@ def batch_form(kernel_name: str, reqs, inputs: dict, warmup: int, steps: int, au
     out = {"value": updates / seconds, "unit": "cell-updates/s", "steps": to_run, "warmup": warm,
            "ms_per_step": seconds / to_run * 1e3, "form": FORM_NAMES[kernel_name], "solves": len(reqs),
            "cells_total": sum(cells), "state_bytes": b.bytes, "cell_updates": updates,
-           "z_chunk_limit": zchunk or "default (compact 16, D form 64 planes)",
+           "z_chunk_limit": zchunk or "default", "tuning": b.tuning(),
            "autotune": "fdtd_batch_autotune before timing (its trial steps are excluded)" if autotune else "off",
            "roofline": {"bound": "hbm", "kernel": "batch step (all kernels)", "achieved": bpc * updates / seconds / 1e9,
                         "peak": peak, "unit": "GB/s", "frac": bpc * updates / seconds / 1e9 / peak,

@@ -22,6 +22,9 @@ EXE = PKG / "bin" / "fdtd"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# extra nvcc options, e.g. "-DFDTD_STRIP_STAGES=4" for a build that measures
+# another ring depth (a changed value needs a forced rebuild)
+EXTRA = os.environ.get("FDTD_NVCC_FLAGS", "").split()
 
 CU_SOURCES = ["compat.cu", "native.cu", "step_fused.cu", "step_strip.cu", "batch_strip.cu", "step_static.cu", "solver.cu", "monitor.cu", "batch.cu", "cuda_util.cu"]
 CPP_SOURCES = ["host_io.cpp"]
@@ -54,7 +57,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         objs.append(obj)
         if force or _stale(obj, [CSRC / src] + common_deps):
             jobs.append([NVCC, "-c", "-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xptxas", "-v",
-                         "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{ROOT / 'include'}",
+                         "-Xcompiler", "-fPIC,-ffp-contract=off", f"-I{ROOT / 'include'}", *EXTRA,
                          str(CSRC / src), "-o", str(obj)])
     for src in CPP_SOURCES:
         obj = OBJ / (Path(src).stem + ".o")
