@@ -252,6 +252,7 @@ int rebuild(fdtd_batch *b)
         std::memset(&d, 0, sizeof d);
         for (int par = 0; par < 2; par++) {
             d.c[par] = solve_consts(v, par, b->d_work + BATCH_ERR_WORD);
+            d.c[par].fuse_mur_x = strip ? 1 : 0;  // the strip kernel applies the x-face Mur updates
             if (strip ? !strip::encode_strip_maps(d.c[par], b->r16, ty, &d.smaps[par])
                       : !encode_step_maps(d.c[par], b->compact, &d.maps[par], b->r16))
                 return FDTD_ERR_INVALID;
@@ -266,11 +267,19 @@ int rebuild(fdtd_batch *b)
         d.unit_count = d.tiles_x * d.tiles_y * d.chunks;
         d.steps_target = v->steps_target;
         units += d.unit_count;
+        const int fused = mur_x_fused_faces(d.c[0]);
         for (int f = 0; f < 12; f++) {
             const MurFace m = mur_face(f, v->nx, v->ny, v->nz);
-            const long long cells = (long long)m.len_u * m.len_v;
+            long long cells = (long long)m.len_u * m.len_v;
+            int limit = 0;
+            if (m.axis == 0 && (fused & (m.far ? 2 : 1))) {
+                if (m.comp == 1)
+                    continue;  // ey x face: updated by the step kernel
+                cells = m.len_u;  // ez x face: only the z = 0 row is left
+                limit = m.len_u;
+            }
             for (long long first = 0; first < cells; first += BATCH_MUR_CELLS)
-                mur.push_back(BatchMurBlock{(int)i, f, (int)first, 0});
+                mur.push_back(BatchMurBlock{(int)i, f, (int)first, limit});
         }
     }
     // new solves: the batch stream waits for their uploads on the side stream

@@ -14,8 +14,8 @@ namespace fdtd {
 namespace strip {
 namespace {
 
-template <int RY, int W, int S, bool R16>
-__global__ void __launch_bounds__(32 * W) batch_strip_kernel(const BatchDesc *__restrict__ descs, int nsolves,
+template <int RY, int W, int S, bool R16, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) batch_strip_kernel(const BatchDesc *__restrict__ descs, int nsolves,
                                                              int total_units, int *work_counter,
                                                              const unsigned long long *__restrict__ memless)
 {
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(32 * W) batch_strip_kernel(const BatchDesc *__
 template <int SHAPE, bool R16>
 struct BatchKernel {
     static constexpr int RY = Shape<SHAPE>::RY, W = Shape<SHAPE>::W;
-    static constexpr auto fn = batch_strip_kernel<RY, W, S_SEL, R16>;
+    static constexpr auto fn = batch_strip_kernel<RY, W, S_SEL, R16, Shape<SHAPE>::BATCH_CTAS>;
     static int smem(int nclasses) { return strip_smem_bytes<RY, W, S_SEL, R16>(nclasses); }
     // the shared-memory opt-in holds for the current device only
     static int opt_in()

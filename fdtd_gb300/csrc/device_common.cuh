@@ -243,13 +243,17 @@ template <int K>
 __device__ __forceinline__ void mur_apply_flat_k(int f, unsigned idx0, unsigned stride, int nx, int ny, int nz,
                                                  int pitch, float dt, float hx, float hy, float hz, float me,
                                                  const MurSlabs &rp, float *t0, float *t1, float *t2,
-                                                 const float *s0, const float *s1, const float *s2, bool fix_ey)
+                                                 const float *s0, const float *s1, const float *s2, bool fix_ey,
+                                                 unsigned limit = 0)
 {
     const MurSet ms(f, nx, ny, nz, hx, hy, hz, rp, t0, t1, t2, s0, s1, s2, fix_ey);
     const MurFace &m = ms.m;
     if (m.len_u <= 0 || m.len_v <= 0)
         return;
-    const unsigned lu = (unsigned)m.len_u, total = lu * (unsigned)m.len_v;
+    const unsigned lu = (unsigned)m.len_u;
+    unsigned total = lu * (unsigned)m.len_v;
+    if (limit > 0 && limit < total)  // only the set's first `limit` cells (rows of u)
+        total = limit;
     float rs[K], rn[K], tn[K], sn[K], sf[K];
     size_t face[K];
     bool on[K];

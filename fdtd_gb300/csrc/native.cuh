@@ -165,11 +165,13 @@ struct alignas(64) BatchDesc {
 };
 
 // One face block of the batched Mur launch: solve, face set, first cell;
-// a block of 256 threads updates BATCH_MUR_CELLS consecutive cells of the set.
+// a block of 256 threads updates BATCH_MUR_CELLS consecutive cells of the set
+// (up to `limit`).
 constexpr int BATCH_MUR_CELLS = 1024;
 static_assert(BATCH_MUR_CELLS % 256 == 0, "whole cells per thread");
 struct BatchMurBlock {
-    int solve, face, first, pad;
+    int solve, face, first;
+    int limit;  // update only the set's first `limit` cells (0: all)
 };
 
 struct BatchLaunch {

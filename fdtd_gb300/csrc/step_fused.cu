@@ -745,7 +745,7 @@ __global__ void __launch_bounds__(256) batch_mur_kernel(const BatchDesc *__restr
     mur_apply_flat_k<BATCH_MUR_CELLS / 256>(b.face, (unsigned)b.first + threadIdx.x, 256u, c.nx, c.ny, c.nz, c.pitch,
                                             c.dt, c.hx, c.hy, c.hz, c.me, c.rp, c.e_prev[0], c.e_prev[1],
                                             c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
-                                            c.scheme == FDTD_SCHEME_CORRECTED);
+                                            c.scheme == FDTD_SCHEME_CORRECTED, (unsigned)b.limit);
 }
 
 __global__ void batch_advance_kernel(const BatchDesc *__restrict__ descs, int nsolves, int *work_counter)

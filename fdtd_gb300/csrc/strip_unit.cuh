@@ -79,10 +79,13 @@ struct StripGeo {
 // (the same shared memory per CTA, 4, 8 or 2 warps), 3 uses 16-row tiles.
 constexpr int STRIP_SHAPES = 4;
 template <int SHAPE> struct Shape;
-template <> struct Shape<0> { static constexpr int RY = 2, W = 4; };
-template <> struct Shape<1> { static constexpr int RY = 1, W = 8; };
-template <> struct Shape<2> { static constexpr int RY = 4, W = 2; };
-template <> struct Shape<3> { static constexpr int RY = 4, W = 4; };
+// BATCH_CTAS: resident CTAs per SM the persistent batched kernel is built
+// for (its register bound; the solve's constants come from shared memory
+// there, which without a bound costs it 100-160 registers).
+template <> struct Shape<0> { static constexpr int RY = 2, W = 4, BATCH_CTAS = 5; };
+template <> struct Shape<1> { static constexpr int RY = 1, W = 8, BATCH_CTAS = 4; };
+template <> struct Shape<2> { static constexpr int RY = 4, W = 2, BATCH_CTAS = 8; };
+template <> struct Shape<3> { static constexpr int RY = 4, W = 4, BATCH_CTAS = 2; };
 
 #ifndef FDTD_STRIP_STAGES
 #define FDTD_STRIP_STAGES 3
@@ -125,23 +128,33 @@ __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy
 
 // One thread arms the stage's barrier and issues the plane's boxes; no_r:
 // the tile-plane holds no Debye memory, its R (and scale words) are not
-// loaded.  With arm_only (the stall test hook) nothing is issued.
+// loaded.  With arm_only (the stall test hook) nothing is issued.  part:
+// ISSUE_ALL, or the plane in two parts on one barrier -- ISSUE_HALO arms it
+// for the whole plane and issues the E^n and H boxes (the H pass's inputs),
+// ISSUE_TILE later issues the classes, R and scale words (the E pass's).
+enum StripIssuePart { ISSUE_ALL = 0, ISSUE_HALO = 1, ISSUE_TILE = 2 };
+
 template <int RY, int W, bool R16>
 __device__ __forceinline__ void strip_issue(const StripMaps &maps, unsigned char *stage, uint32_t bar, int kind,
-                                            int x0, int y0, int z, bool arm_only, bool no_r)
+                                            int x0, int y0, int z, bool arm_only, bool no_r, int part = ISSUE_ALL)
 {
     using G = StripGeo<RY, W, R16>;
-    const unsigned full = no_r ? G::TX_FULL - 3u * G::R_BYTES - G::X_BYTES : G::TX_FULL;
-    mbar_expect_tx(bar, kind == PLANE_FULL ? full : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI));
-    if (arm_only)
-        return;
-    for (int c = 0; c < 3; c++)
-        tma_load_3d(smem_addr(stage + G::OFF_E + c * pad128(G::E_BYTES)), &maps.m[c], x0 - 4, y0 - 1, z, bar);
-    if (kind == PLANE_EPI)
-        return;
-    for (int c = 0; c < 3; c++)
-        tma_load_3d(smem_addr(stage + G::OFF_H + c * pad128(G::H_BYTES)), &maps.m[3 + c], x0 - 4, y0 - 1, z, bar);
-    if (kind == PLANE_PRO)
+    if (part != ISSUE_TILE) {
+        const unsigned full = no_r ? G::TX_FULL - 3u * G::R_BYTES - G::X_BYTES : G::TX_FULL;
+        mbar_expect_tx(bar, kind == PLANE_FULL ? full : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI));
+        if (arm_only)
+            return;
+        for (int c = 0; c < 3; c++)
+            tma_load_3d(smem_addr(stage + G::OFF_E + c * pad128(G::E_BYTES)), &maps.m[c], x0 - 4, y0 - 1, z, bar);
+        if (kind == PLANE_EPI)
+            return;
+        for (int c = 0; c < 3; c++)
+            tma_load_3d(smem_addr(stage + G::OFF_H + c * pad128(G::H_BYTES)), &maps.m[3 + c], x0 - 4, y0 - 1, z,
+                        bar);
+        if (part == ISSUE_HALO)
+            return;
+    }
+    if (kind != PLANE_FULL)
         return;
     tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[9], x0, y0, z, bar);
     if (no_r)
@@ -298,6 +311,8 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
         // ---- H^{n+1/2} at plane z on the strip (fdtd_calculations.cu:43-76)
         float ex[RY + 1], ey[RY], ez[RY + 1];
         float hxn[RY], hyn[RY], hzn[RY];
+        float ey_nb[RY], ez_nb[RY];  // face lanes: E^n y, z of the x-neighbour (read here: the box is
+                                     // refilled before the E pass)
 #pragma unroll
         for (int r = 0; r <= RY; r++) {
             ex[r] = ea(0, ry0 + r + 1, ec);
@@ -311,6 +326,11 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             hyn[r] = ha(1, er, ec);
             hzn[r] = ha(2, er, ec);
             const int y = y0 + ry0 + r;
+            if (face_cta) {
+                const int cn = face_far ? ec - 1 : ec + 1;
+                ey_nb[r] = ea(1, er, cn);
+                ez_nb[r] = ea(2, er, cn);
+            }
             if (fast) {
                 hxn[r] = cm_h(hxn[r], ky, ez[r + 1], ez[r], ky, eb(1, er, ec), ey[r]);
                 hyn[r] = cm_h(hyn[r], kz, eb(0, er, ec), ex[r], kx, ea(2, er, ec + 1), ez[r]);
@@ -388,6 +408,14 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             if (__syncthreads_or(!ok)) {
                 give_up(k);
                 return false;
+            }
+            // the H pass has consumed this stage's E^n and H boxes: refill
+            // them with plane k + S now, half a plane before the rest
+            if (tid == 0 && k + S < nplanes) {
+                fence_async_shared();
+                const int zn = p0 + k + S;
+                strip_issue<RY, W, R16>(maps, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
+                                        no_r(zn), ISSUE_HALO);
             }
 
             // ---- D increment, sources, E^{n+1} and R^{n+1} on the strip
@@ -491,19 +519,18 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
                         const float ey_lo = __shfl_up_sync(all, en1, 1), ez_lo = __shfl_up_sync(all, en2, 1);
                         if (face_lane && y < ny && zmid) {
                             const float4 mf = c.mur_x[((size_t)(face_far ? 1 : 0) * nz + z) * ny + y];
-                            const int er = row + 1, cn = face_far ? ec - 1 : ec + 1;
                             auto mur = [&](float tn, float sn, float sf) {
                                 return __fmul_rn(mf.x, __fsub_rn(__fadd_rn(__fmul_rn(mf.y, tn), __fmul_rn(mf.z, sn)),
                                                                  __fmul_rn(mf.w, sf)));
                             };
                             if (y <= ny - 2) {  // ey faces: y 0..ny-2, z 1..nz-2
                                 // fdtd_calculations.cu:323: the far ey face reads E^n at x-1 in both terms
-                                const float tn = face_far ? (c.scheme == FDTD_SCHEME_CORRECTED ? ey_lo : ea(1, er, cn))
+                                const float tn = face_far ? (c.scheme == FDTD_SCHEME_CORRECTED ? ey_lo : ey_nb[r])
                                                           : ey_hi;
-                                en1 = mur(tn, ea(1, er, cn), ey[r]);
+                                en1 = mur(tn, ey_nb[r], ey[r]);
                             }
                             if (y >= 1 && y <= ny - 2)  // ez faces: y 1..ny-2 (z = 0 in the Mur kernel)
-                                en2 = mur(face_far ? ez_lo : ez_hi, ea(2, er, cn), ez[r]);
+                                en2 = mur(face_far ? ez_lo : ez_hi, ez_nb[r], ez[r]);
                         }
                     }
                 }
@@ -552,12 +579,13 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
                 bulk_commit();  // its reads of the output set are waited for before the next plane writes
             }
         }
-        // refill the stage of plane k with plane k + S
+        // refill the stage of plane k with plane k + S: all of it after a
+        // prologue plane, its classes, R and scale words after a full plane
         if (tid == 0 && k + S < nplanes) {
             fence_async_shared();
             const int zn = p0 + k + S;
             strip_issue<RY, W, R16>(maps, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
-                                    no_r(zn));
+                                    no_r(zn), z < zc0 ? ISSUE_ALL : ISSUE_TILE);
         }
     }
     return true;
