@@ -566,7 +566,45 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             }
             fence_async_shared();
             __syncthreads();  // stage k consumed, output tiles written
+#ifdef FDTD_STRIP_COPY_OUT
+            // measurement build: every thread copies part of the output
+            // tiles to global memory with 16-byte stores instead of the
+            // TMA stores
+            {
+                constexpr int RF4 = SX / 4;  // float4 per tile row
+                const size_t zoff = (size_t)z * c.ny * c.pitch;
+                const int nft = 6 + ((!R16 && !plane_no_r) ? 3 : 0);
+                for (int i = tid; i < nft * TY * RF4; i += G::NTH) {
+                    const int ti = i / (TY * RF4), rem = i % (TY * RF4), rr = rem / RF4, q = rem % RF4;
+                    const int yy = y0 + rr, xx = x0 + 4 * q;
+                    if (yy >= ny || xx >= nx)
+                        continue;
+                    float *dst = ti < 3 ? c.h_out[ti] : (ti < 6 ? c.e_prev[ti - 3] : c.d_prev[ti - 6]);
+                    const int so = ti < 3 ? G::O_H + ti * G::T_BYTES
+                                          : (ti < 6 ? G::O_E + (ti - 3) * G::T_BYTES : G::O_R + (ti - 6) * pad128(G::R_BYTES));
+                    *reinterpret_cast<float4 *>(dst + zoff + (size_t)yy * c.pitch + xx) =
+                        reinterpret_cast<const float4 *>(O + so)[rr * RF4 + q];
+                }
+                if (R16 && !plane_no_r) {
+                    constexpr int HF4 = SX / 8;  // float4 per row of FP16 values
+                    for (int i = tid; i < 3 * TY * HF4; i += G::NTH) {
+                        const int ti = i / (TY * HF4), rem = i % (TY * HF4), rr = rem / HF4, q = rem % HF4;
+                        const int yy = y0 + rr, xx = x0 + 8 * q;
+                        if (yy >= ny || xx >= nx)
+                            continue;
+                        unsigned short *dst = reinterpret_cast<unsigned short *>(c.d_prev[ti]);
+                        *reinterpret_cast<float4 *>(dst + zoff + (size_t)yy * c.pitch + xx) =
+                            reinterpret_cast<const float4 *>(O + G::O_R + ti * pad128(G::R_BYTES))[rr * HF4 + q];
+                    }
+                    if (tid < TY && y0 + tid < ny)
+                        c.r_exp[((size_t)z * r16_segments(nx) + x0 / SX) * r16_rows(ny) + y0 + tid] =
+                            reinterpret_cast<const uint32_t *>(O + G::O_X)[tid];
+                }
+            }
+            if (false) {
+#else
             if (tid == G::STORE_TID) {
+#endif
                 const uint32_t ob = smem_addr(O);
                 for (int comp = 0; comp < 3; comp++) {
                     tma_store_3d(&maps.m[11 + comp], ob + G::O_H + comp * G::T_BYTES, x0, y0, z);
