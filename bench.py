@@ -103,7 +103,7 @@ def parse_args():
     ap.add_argument("--ref-seconds", type=float, default=150.0,
                     help="--impl reference: most seconds of timed CPU steps (fewer steps than --steps if needed)")
     ap.add_argument("--forms-batch-steps", type=int, default=300,
-                    help="timed steps of the batched forms in the default run")
+                    help="timed steps of the batched forms in the default run (0: skip them)")
     ap.add_argument("--forms-serve-seconds", type=float, default=10.0,
                     help="arrival window of the served form in the default run (20 req/s; 0: skip)")
     ap.add_argument("--no-precision", action="store_true",
@@ -503,7 +503,7 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
                                                               args.scheme)
     # ---- the batched (64 uneven solves, both storage forms) and served
     # (request stream, 16-bit form) forms, N = 1 only
-    if args.kernel == "single" and not args.no_forms and world == 1:
+    if args.kernel == "single" and not args.no_forms and world == 1 and args.forms_batch_steps > 0:
         reqs = batch_requests(64)
         btmp = tempfile.TemporaryDirectory()
         binputs = _request_inputs(reqs, Path(btmp.name))
@@ -511,8 +511,8 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
                           for k in ("compact", "compact16")}
         del binputs
         btmp.cleanup()
-        if args.forms_serve_seconds > 0:
-            forms["serve"] = serve_form("compact16", 20.0, args.forms_serve_seconds)
+    if args.kernel == "single" and not args.no_forms and world == 1 and args.forms_serve_seconds > 0:
+        forms["serve"] = serve_form("compact16", 20.0, args.forms_serve_seconds)
 
     # ---- end to end through the C ABI with host buffers (e2e)
     e2e = None

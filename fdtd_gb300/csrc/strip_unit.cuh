@@ -47,7 +47,6 @@ constexpr int SX = 32;  // tile width in x: one warp's lanes
 template <int RY, int W, bool R16>
 struct StripGeo {
     static constexpr int TY = RY * W, NTH = 32 * W;
-    static constexpr int STORE_TID = W > 1 ? 32 : 0;  // lane 0 of warp 1 issues the stores (thread 0 the loads)
     static_assert(TY % 4 == 0 && TY <= 32, "tile rows: a multiple of 4 (scale-word boxes) and one lane per row");
     static constexpr int EW = SX + 8, EH = TY + 2;  // E^n box: x0-4 .. x0+35, y0-1 .. y0+TY
     static constexpr int HW = SX + 4, HH = TY + 1;  // H box: x0-4 .. x0+31, y0-1 .. y0+TY-1
@@ -68,7 +67,16 @@ struct StripGeo {
     static constexpr int T_BYTES = SX * TY * 4;
     static constexpr int O_H = 0, O_E = 3 * T_BYTES, O_R = 6 * T_BYTES;
     static constexpr int O_X = O_R + 3 * pad128(R_BYTES);
-    static constexpr int OUT = pad128(O_X + X_BYTES);
+    // Where the output tiles live: in the plane's own ring stage, over its
+    // E^n and H boxes (consumed by the H pass), when they fit below the
+    // stage's R tiles; else in an area of their own.  In the stage they cost
+    // no shared memory (one more CTA per SM), but the stage's refill waits
+    // for its stores to have read them.
+    static constexpr bool IN_STAGE = O_X + X_BYTES <= OFF_R;
+    static constexpr int OUT = IN_STAGE ? 0 : pad128(O_X + X_BYTES);
+    // the thread that issues the TMA stores: thread 0, which also issues the
+    // loads, when a stage's refill waits for its stores; else lane 0 of warp 1
+    static constexpr int STORE_TID = (W > 1 && !IN_STAGE) ? 32 : 0;
     // H^{n+1/2} hz, hy of every row with the x0-1 column in front ([2][TY][33]),
     // and hz, hx of the row above each warp's first row ([2][W][32]; row
     // y0-1 for warp 0)
@@ -401,17 +409,19 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             }
             // the CTA decides here whether a wait gave up (nothing has
             // reached global memory from this plane yet)
-            // the output tiles this plane writes were stored one plane ago:
-            // that store has read them by now (checked before the barrier)
-            if (tid == G::STORE_TID)
+            // outputs in their own area: the tiles this plane writes were
+            // stored one plane ago, and that store has read them by now
+            // (checked before the barrier)
+            if (!G::IN_STAGE && tid == G::STORE_TID)
                 bulk_wait_read<0>();
             if (__syncthreads_or(!ok)) {
                 give_up(k);
                 return false;
             }
-            // the H pass has consumed this stage's E^n and H boxes: refill
-            // them with plane k + S now, half a plane before the rest
-            if (tid == 0 && k + S < nplanes) {
+            // outputs in their own area: the H pass has consumed this
+            // stage's E^n and H boxes, refill them with plane k + S now, half
+            // a plane before the rest
+            if (!G::IN_STAGE && tid == 0 && k + S < nplanes) {
                 fence_async_shared();
                 const int zn = p0 + k + S;
                 strip_issue<RY, W, R16>(maps, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
@@ -420,7 +430,7 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
 
             // ---- D increment, sources, E^{n+1} and R^{n+1} on the strip
             const bool plane_no_r = no_r(z);  // uniform: R is +0 on every cell of the tile-plane
-            unsigned char *O = sm.outs;
+            unsigned char *O = G::IN_STAGE ? stage(k) : sm.outs;
             float *OH = reinterpret_cast<float *>(O + G::O_H);
             float *OE = reinterpret_cast<float *>(O + G::O_E);
             const unsigned char *M = stage(k) + G::OFF_M;
@@ -566,45 +576,7 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             }
             fence_async_shared();
             __syncthreads();  // stage k consumed, output tiles written
-#ifdef FDTD_STRIP_COPY_OUT
-            // measurement build: every thread copies part of the output
-            // tiles to global memory with 16-byte stores instead of the
-            // TMA stores
-            {
-                constexpr int RF4 = SX / 4;  // float4 per tile row
-                const size_t zoff = (size_t)z * c.ny * c.pitch;
-                const int nft = 6 + ((!R16 && !plane_no_r) ? 3 : 0);
-                for (int i = tid; i < nft * TY * RF4; i += G::NTH) {
-                    const int ti = i / (TY * RF4), rem = i % (TY * RF4), rr = rem / RF4, q = rem % RF4;
-                    const int yy = y0 + rr, xx = x0 + 4 * q;
-                    if (yy >= ny || xx >= nx)
-                        continue;
-                    float *dst = ti < 3 ? c.h_out[ti] : (ti < 6 ? c.e_prev[ti - 3] : c.d_prev[ti - 6]);
-                    const int so = ti < 3 ? G::O_H + ti * G::T_BYTES
-                                          : (ti < 6 ? G::O_E + (ti - 3) * G::T_BYTES : G::O_R + (ti - 6) * pad128(G::R_BYTES));
-                    *reinterpret_cast<float4 *>(dst + zoff + (size_t)yy * c.pitch + xx) =
-                        reinterpret_cast<const float4 *>(O + so)[rr * RF4 + q];
-                }
-                if (R16 && !plane_no_r) {
-                    constexpr int HF4 = SX / 8;  // float4 per row of FP16 values
-                    for (int i = tid; i < 3 * TY * HF4; i += G::NTH) {
-                        const int ti = i / (TY * HF4), rem = i % (TY * HF4), rr = rem / HF4, q = rem % HF4;
-                        const int yy = y0 + rr, xx = x0 + 8 * q;
-                        if (yy >= ny || xx >= nx)
-                            continue;
-                        unsigned short *dst = reinterpret_cast<unsigned short *>(c.d_prev[ti]);
-                        *reinterpret_cast<float4 *>(dst + zoff + (size_t)yy * c.pitch + xx) =
-                            reinterpret_cast<const float4 *>(O + G::O_R + ti * pad128(G::R_BYTES))[rr * HF4 + q];
-                    }
-                    if (tid < TY && y0 + tid < ny)
-                        c.r_exp[((size_t)z * r16_segments(nx) + x0 / SX) * r16_rows(ny) + y0 + tid] =
-                            reinterpret_cast<const uint32_t *>(O + G::O_X)[tid];
-                }
-            }
-            if (false) {
-#else
             if (tid == G::STORE_TID) {
-#endif
                 const uint32_t ob = smem_addr(O);
                 for (int comp = 0; comp < 3; comp++) {
                     tma_store_3d(&maps.m[11 + comp], ob + G::O_H + comp * G::T_BYTES, x0, y0, z);
@@ -614,16 +586,19 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
                 }
                 if (R16 && !plane_no_r)
                     tma_store_3d(&maps.m[10], ob + G::O_X, y0, x0 / SX, z);
-                bulk_commit();  // its reads of the output set are waited for before the next plane writes
+                bulk_commit();
+                if (G::IN_STAGE)  // the refill below overwrites the tiles
+                    bulk_wait_read<0>();
             }
         }
         // refill the stage of plane k with plane k + S: all of it after a
-        // prologue plane, its classes, R and scale words after a full plane
+        // prologue plane or with the outputs in the stage, else its classes,
+        // R and scale words (the boxes went after the H pass)
         if (tid == 0 && k + S < nplanes) {
             fence_async_shared();
             const int zn = p0 + k + S;
             strip_issue<RY, W, R16>(maps, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
-                                    no_r(zn), z < zc0 ? ISSUE_ALL : ISSUE_TILE);
+                                    no_r(zn), (z < zc0 || G::IN_STAGE) ? ISSUE_ALL : ISSUE_TILE);
         }
     }
     return true;
