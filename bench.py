@@ -715,7 +715,7 @@ def run_batch_workload(args) -> None:
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"batch of {len(reqs)} solves, dims log-uniform 48-256 per axis, 1-4 Debye "
                                f"ellipsoids, source U[0.3,3] GHz, steps U[500,3000], corrected scheme, {f['form']}",
-                   **{k: f[k] for k in ("solves", "cells_total", "state_bytes", "cell_updates", "z_chunk_limit",
+                   **{k: f[k] for k in ("solves", "cells_total", "state_bytes", "cell_updates", "z_chunk_limit", "tuning",
                                         "autotune")}, "l2": "state >> 129 MB L2: no flush"},
         "roofline": {**f["roofline"], "traffic": None}, "gpu_launches": f["gpu_launches"], "clocks": f["clocks"],
         "e2e": None, "cpu_baseline": None}

@@ -81,7 +81,8 @@ __global__ void __launch_bounds__(32 * W, MINB) batch_strip_kernel(const BatchDe
 template <int SHAPE, bool R16>
 struct BatchKernel {
     static constexpr int RY = Shape<SHAPE>::RY, W = Shape<SHAPE>::W;
-    static constexpr auto fn = batch_strip_kernel<RY, W, S_SEL, R16, Shape<SHAPE>::BATCH_CTAS>;
+    static constexpr int MINB = R16 ? Shape<SHAPE>::BATCH_CTAS16 : Shape<SHAPE>::BATCH_CTAS32;
+    static constexpr auto fn = batch_strip_kernel<RY, W, S_SEL, R16, MINB>;
     static int smem(int nclasses) { return strip_smem_bytes<RY, W, S_SEL, R16>(nclasses); }
     // the shared-memory opt-in holds for the current device only
     static int opt_in()
