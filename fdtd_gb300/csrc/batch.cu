@@ -116,7 +116,7 @@ struct fdtd_batch {
     std::map<int, cudaGraphExec_t> graphs;  // steps per graph -> exec
     size_t bytes = 0;
     int zchunk_max = 0;  // largest z chunk (fdtd_batch_autotune); 0: the form's default
-    int strip_shape = 1;  // compact forms: strip kernel shape, -1 the z-marching kernel (fdtd_batch_autotune)
+    int strip_shape = 0;  // compact forms: strip kernel shape, -1 the z-marching kernel (fdtd_batch_autotune)
     bool strip = false;   // the current launch runs the strip kernel
     unsigned long long *d_memless = nullptr;  // per unit: planes whose tile has no Debye memory
     size_t memless_cap = 0;

@@ -59,7 +59,11 @@ struct StripGeo {
     static constexpr int OFF_R = OFF_H + 3 * pad128(H_BYTES);
     static constexpr int OFF_X = OFF_R + 3 * pad128(R_BYTES);
     static constexpr int OFF_M = OFF_X + pad128(X_BYTES);
-    static constexpr int STAGE = pad128(OFF_M + M_BYTES);
+    // x-face tiles: the Mur factors of the tile's rows, near face then far
+    // face ([2][TY] float4)
+    static constexpr int F_BYTES = 2 * TY * 16;
+    static constexpr int OFF_F = pad128(OFF_M + M_BYTES);
+    static constexpr int STAGE = pad128(OFF_F + F_BYTES);
     static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 3u * R_BYTES + X_BYTES + M_BYTES;
     static constexpr unsigned TX_PRO = 3u * E_BYTES + 3u * H_BYTES;
     static constexpr unsigned TX_EPI = 3u * E_BYTES;
@@ -142,16 +146,28 @@ __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy
 // loaded.  With arm_only (the stall test hook) nothing is issued.  part:
 // ISSUE_ALL, or the plane in two parts on one barrier -- ISSUE_HALO arms it
 // for the whole plane and issues the E^n and H boxes (the H pass's inputs),
-// ISSUE_TILE later issues the classes, R and scale words (the E pass's).
+// ISSUE_TILE later issues the classes, R, scale words and x-face Mur
+// factors (the E pass's).
 enum StripIssuePart { ISSUE_ALL = 0, ISSUE_HALO = 1, ISSUE_TILE = 2 };
 
+// A face tile's Mur factors: rows y0 .. of plane 0 of the near and far x face
+// (nullptr: the tile does not hold that face); plane z lies z * plane float4
+// further on.  bytes: the rows inside the grid x 16 (one copy), tx: the bytes
+// of both copies.
+struct StripFaces {
+    const float4 *near, *far;
+    size_t plane;
+    uint32_t bytes, tx;
+};
+
 template <int RY, int W, bool R16>
-__device__ __forceinline__ void strip_issue(const StripMaps &maps, unsigned char *stage, uint32_t bar, int kind,
-                                            int x0, int y0, int z, bool arm_only, bool no_r, int part = ISSUE_ALL)
+__device__ __forceinline__ void strip_issue(const StripMaps &maps, const StripFaces &f, unsigned char *stage,
+                                            uint32_t bar, int kind, int x0, int y0, int z, bool arm_only, bool no_r,
+                                            int part = ISSUE_ALL)
 {
     using G = StripGeo<RY, W, R16>;
     if (part != ISSUE_TILE) {
-        const unsigned full = no_r ? G::TX_FULL - 3u * G::R_BYTES - G::X_BYTES : G::TX_FULL;
+        const unsigned full = (no_r ? G::TX_FULL - 3u * G::R_BYTES - G::X_BYTES : G::TX_FULL) + f.tx;
         mbar_expect_tx(bar, kind == PLANE_FULL ? full : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI));
         if (arm_only)
             return;
@@ -168,6 +184,10 @@ __device__ __forceinline__ void strip_issue(const StripMaps &maps, unsigned char
     if (kind != PLANE_FULL)
         return;
     tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[9], x0, y0, z, bar);
+    if (f.near)
+        bulk_load(smem_addr(stage + G::OFF_F), f.near + (size_t)z * f.plane, f.bytes, bar);
+    if (f.far)
+        bulk_load(smem_addr(stage + G::OFF_F + G::TY * 16), f.far + (size_t)z * f.plane, f.bytes, bar);
     if (no_r)
         return;
     for (int c = 0; c < 3; c++)
@@ -259,9 +279,25 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
     auto bar = [&](int k) { return smem_addr(&sm.bars[(g0 + k) % S]); };
     auto parity = [&](int k) { return (uint32_t)(((g0 + k) / S) & 1); };
     auto no_r = [&](int z) { return z >= zc0 && ((memless >> (z - zc0)) & 1ull) != 0; };
+    // x-face Mur updates (updateMurBoundary ey/ez x faces,
+    // fdtd_calculations.cu:280-340) in the tiles that hold x = 0 or nx-1;
+    // their per-cell factors arrive with the plane's boxes
+    const int mur_bits = mur_x_fused_faces(c);
+    const bool face_near = (mur_bits & 1) && x0 == 0;
+    const bool face_far_cta = (mur_bits & 2) && x0 <= nx - 1 && nx - 1 < x0 + SX;
+    const bool face_cta = face_near || face_far_cta;
+    StripFaces faces{nullptr, nullptr, (size_t)ny, 0u, 0u};
+    if (face_cta) {
+        faces.bytes = (uint32_t)min(TY, ny - y0) * 16u;
+        if (face_near)
+            faces.near = c.mur_x + y0;
+        if (face_far_cta)
+            faces.far = c.mur_x + (size_t)nz * ny + y0;
+        faces.tx = (face_near ? faces.bytes : 0u) + (face_far_cta ? faces.bytes : 0u);
+    }
     if (tid == 0)
         for (int k = 0; k < S && k < nplanes; k++)
-            strip_issue<RY, W, R16>(maps, stage(k), bar(k), plane_kind(p0 + k, zc0, zc1), x0, y0, p0 + k,
+            strip_issue<RY, W, R16>(maps, faces, stage(k), bar(k), plane_kind(p0 + k, zc0, zc1), x0, y0, p0 + k,
                                     stall && k == 1, no_r(p0 + k));
 
     float jz_now = 0.0f;
@@ -272,10 +308,6 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
     }
     const float kx = c.kx, ky = c.ky, kz = c.kz, tcx = c.tx, tcy = c.ty, tcz = c.tz;
     const int cls_max = c.nclasses - 1;
-    // x-face Mur updates (updateMurBoundary ey/ez x faces,
-    // fdtd_calculations.cu:280-340) in the tiles that hold x = 0 or nx-1
-    const int mur_bits = mur_x_fused_faces(c);
-    const bool face_cta = ((mur_bits & 1) && x0 == 0) || ((mur_bits & 2) && x0 <= nx - 1 && nx - 1 < x0 + SX);
     const bool face_far = x == nx - 1;
     const bool face_lane = x < nx && (((mur_bits & 1) && x == 0) || ((mur_bits & 2) && face_far));
     // every own cell and every halo cell inside the update ranges of all
@@ -427,8 +459,8 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
             if (!G::IN_STAGE && tid == 0 && k + S < nplanes) {
                 fence_async_shared();
                 const int zn = p0 + k + S;
-                strip_issue<RY, W, R16>(maps, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
-                                        no_r(zn), ISSUE_HALO);
+                strip_issue<RY, W, R16>(maps, faces, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn,
+                                        false, no_r(zn), ISSUE_HALO);
             }
 
             // ---- D increment, sources, E^{n+1} and R^{n+1} on the strip
@@ -531,7 +563,8 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
                         const float ey_hi = __shfl_down_sync(all, en1, 1), ez_hi = __shfl_down_sync(all, en2, 1);
                         const float ey_lo = __shfl_up_sync(all, en1, 1), ez_lo = __shfl_up_sync(all, en2, 1);
                         if (face_lane && y < ny && zmid) {
-                            const float4 mf = c.mur_x[((size_t)(face_far ? 1 : 0) * nz + z) * ny + y];
+                            const float4 mf =
+                                reinterpret_cast<const float4 *>(stage(k) + G::OFF_F)[(face_far ? TY : 0) + row];
                             auto mur = [&](float tn, float sn, float sf) {
                                 return __fmul_rn(mf.x, __fsub_rn(__fadd_rn(__fmul_rn(mf.y, tn), __fmul_rn(mf.z, sn)),
                                                                  __fmul_rn(mf.w, sf)));
@@ -600,7 +633,7 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
         if (tid == 0 && k + S < nplanes) {
             fence_async_shared();
             const int zn = p0 + k + S;
-            strip_issue<RY, W, R16>(maps, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
+            strip_issue<RY, W, R16>(maps, faces, stage(k + S), bar(k + S), plane_kind(zn, zc0, zc1), x0, y0, zn, false,
                                     no_r(zn), (z < zc0 || G::IN_STAGE) ? ISSUE_ALL : ISSUE_TILE);
         }
     }
