@@ -118,8 +118,8 @@ struct fdtd_batch {
     int zchunk_max = 0;  // largest z chunk (fdtd_batch_autotune); 0: the form's default
     int strip_shape = 0;  // compact forms: strip kernel shape, -1 the z-marching kernel (fdtd_batch_autotune)
     bool strip = false;   // the current launch runs the strip kernel
-    unsigned long long *d_memless = nullptr;  // per unit: planes whose tile has no Debye memory
-    size_t memless_cap = 0;
+    BatchUnit *d_units = nullptr;  // strip kernel: per unit its solve and memoryless planes
+    size_t units_cap = 0;
 };
 
 namespace {
@@ -154,26 +154,45 @@ int pool_alloc(fdtd_batch *b, void **p, size_t bytes, cudaStream_t s)
     return cu(cudaMallocFromPoolAsync(p, bytes, b->pool, s));
 }
 
-// Copies n bytes of host data to dst on the batch stream through the next
-// pinned staging buffer (waiting only for that buffer's previous upload).
-int staged_upload(fdtd_batch *b, void *dst, const void *src, size_t n)
+// One host -> device copy of a table upload.
+struct Upload {
+    void *dst;
+    const void *src;
+    size_t n;
+};
+
+// Copies the tables of one rebuild to the device on the batch stream through
+// the next pinned staging buffer, all in one buffer, so that a rebuild waits
+// only for the upload of the rebuild before the previous one (the buffer's
+// last use), not for the steps queued since.
+int staged_upload(fdtd_batch *b, const std::vector<Upload> &ups)
 {
+    size_t total = 0;
+    for (const Upload &u : ups)
+        total += (u.n + 15) & ~size_t(15);
+    if (total == 0)
+        return FDTD_OK;
     StageBuf &sb = b->stage[b->stage_next];
     b->stage_next ^= 1;
     int st = cu(cudaEventSynchronize(sb.done));
-    if (st == FDTD_OK && sb.cap < n) {
+    if (st == FDTD_OK && sb.cap < total) {
         if (sb.host)
             cudaFreeHost(sb.host);
         sb.host = nullptr;
         sb.cap = 0;
-        const size_t cap = std::max(n, size_t(1) << 20);
+        const size_t cap = std::max(total, size_t(1) << 20);
         st = cu(cudaHostAlloc(&sb.host, cap, cudaHostAllocDefault));
         if (st == FDTD_OK)
             sb.cap = cap;
     }
-    if (st == FDTD_OK) {
-        std::memcpy(sb.host, src, n);
-        st = cu(cudaMemcpyAsync(dst, sb.host, n, cudaMemcpyHostToDevice, b->stream));
+    size_t off = 0;
+    for (const Upload &u : ups) {
+        if (st != FDTD_OK || u.n == 0)
+            continue;
+        unsigned char *h = static_cast<unsigned char *>(sb.host) + off;
+        std::memcpy(h, u.src, u.n);
+        st = cu(cudaMemcpyAsync(u.dst, h, u.n, cudaMemcpyHostToDevice, b->stream));
+        off += (u.n + 15) & ~size_t(15);
     }
     if (st == FDTD_OK)
         st = cu(cudaEventRecord(sb.done, b->stream));
@@ -308,29 +327,39 @@ int rebuild(fdtd_batch *b)
         st = pool_alloc(b, reinterpret_cast<void **>(&b->d_mur), sizeof(BatchMurBlock) * cap, b->stream);
         b->mur_cap = st == FDTD_OK ? cap : 0;
     }
-    // strip kernel: per unit, the planes whose tile holds no Debye memory
-    std::vector<unsigned long long> masks;
+    // strip kernel: per unit its tile, z chunk, solve and the planes whose
+    // tile holds no Debye memory
+    std::vector<BatchUnit> recs;
     if (strip) {
-        masks.assign((size_t)units, 0ull);
+        std::vector<unsigned long long> masks((size_t)units, 0ull);
+        recs.resize((size_t)units);
         for (size_t i = 0; i < b->solves.size(); i++) {
             const BatchSolve *v = b->solves[i];
-            strip_unit_masks(v->memless8, v->nx, v->ny, v->nz, ty, descs[i].zchunk, masks.data() + descs[i].unit_begin);
+            const BatchDesc &d = descs[i];
+            if (d.tiles_x > 65535 || d.tiles_y > 65535 || d.chunks > 65535 || d.zchunk > 65535)
+                return FDTD_ERR_INVALID;
+            strip_unit_masks(v->memless8, v->nx, v->ny, v->nz, ty, d.zchunk, masks.data() + d.unit_begin);
+            for (int j = 0; j < d.unit_count; j++) {
+                const int per_z = d.tiles_x * d.tiles_y, rem = j % per_z;
+                recs[(size_t)d.unit_begin + j] =
+                    BatchUnit{masks[(size_t)d.unit_begin + j], v->counter,           (int)i,
+                              (unsigned short)(rem % d.tiles_x), (unsigned short)(rem / d.tiles_x),
+                              (unsigned short)(j / per_z),       (unsigned short)d.zchunk, d.steps_target};
+            }
         }
-        if (st == FDTD_OK && masks.size() > b->memless_cap) {
-            if (b->d_memless)
-                cudaFreeAsync(b->d_memless, b->stream);
-            b->d_memless = nullptr;
-            const size_t cap = std::max(masks.size() * 2, size_t(1024));
-            st = pool_alloc(b, reinterpret_cast<void **>(&b->d_memless), sizeof(unsigned long long) * cap, b->stream);
-            b->memless_cap = st == FDTD_OK ? cap : 0;
+        if (st == FDTD_OK && recs.size() > b->units_cap) {
+            if (b->d_units)
+                cudaFreeAsync(b->d_units, b->stream);
+            b->d_units = nullptr;
+            const size_t cap = std::max(recs.size() * 2, size_t(1024));
+            st = pool_alloc(b, reinterpret_cast<void **>(&b->d_units), sizeof(BatchUnit) * cap, b->stream);
+            b->units_cap = st == FDTD_OK ? cap : 0;
         }
     }
-    if (st == FDTD_OK && !descs.empty())
-        st = staged_upload(b, b->d_descs, descs.data(), sizeof(BatchDesc) * descs.size());
-    if (st == FDTD_OK && !mur.empty())
-        st = staged_upload(b, b->d_mur, mur.data(), sizeof(BatchMurBlock) * mur.size());
-    if (st == FDTD_OK && !masks.empty())
-        st = staged_upload(b, b->d_memless, masks.data(), sizeof(unsigned long long) * masks.size());
+    if (st == FDTD_OK)
+        st = staged_upload(b, {Upload{b->d_descs, descs.data(), sizeof(BatchDesc) * descs.size()},
+                               Upload{b->d_mur, mur.data(), sizeof(BatchMurBlock) * mur.size()},
+                               Upload{b->d_units, recs.data(), sizeof(BatchUnit) * recs.size()}});
     if (st != FDTD_OK)
         return st;
     int max_classes = 1;
@@ -342,7 +371,7 @@ int rebuild(fdtd_batch *b)
         return FDTD_ERR_INVALID;
     b->launch = BatchLaunch{b->d_descs, (int)descs.size(), units, b->d_work, b->d_mur, (int)mur.size(), ctas,
                             b->compact ? 1 : 0, max_classes, b->r16 ? 1 : 0, strip ? 1 : 0, b->strip_shape,
-                            strip ? b->d_memless : nullptr};
+                            strip ? b->d_units : nullptr};
     b->strip = strip;
     drop_graphs(b);
     b->dirty = false;
@@ -482,8 +511,8 @@ int fdtd_batch_destroy(fdtd_batch *b)
         cudaFreeAsync(b->d_descs, s);
     if (b->d_mur)
         cudaFreeAsync(b->d_mur, s);
-    if (b->d_memless)
-        cudaFreeAsync(b->d_memless, s);
+    if (b->d_units)
+        cudaFreeAsync(b->d_units, s);
     if (s)
         cudaStreamSynchronize(s);
     cudaFree(b->d_work);

@@ -15,62 +15,77 @@ namespace strip {
 namespace {
 
 template <int RY, int W, int S, bool R16, int MINB>
-__global__ void __launch_bounds__(32 * W, MINB) batch_strip_kernel(const BatchDesc *__restrict__ descs, int nsolves,
-                                                             int total_units, int *work_counter,
-                                                             const unsigned long long *__restrict__ memless)
+__global__ void __launch_bounds__(32 * W, MINB) batch_strip_kernel(const BatchDesc *__restrict__ descs,
+                                                                   int total_units, int *work_counter,
+                                                                   const BatchUnit *__restrict__ units)
 {
     using G = StripGeo<RY, W, R16>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    __shared__ NativeConsts s_c;
-    __shared__ int s_unit, s_solve;
+    __shared__ StripConsts s_c;
+    __shared__ BatchUnit s_rec[2];  // the current unit's record and the next one's
+    __shared__ int s_unit, s_n;
     const StripSmem sm = strip_smem<RY, W, S, R16>(smem_raw);
     strip_init_bars<S>(sm);
     const int tid = threadIdx.x;
-    int loaded = -1;
-    unsigned g = 0;  // planes staged by this CTA so far
-    __syncthreads();
-    for (;;) {
+    int loaded = -1;    // solve * 2 + parity whose constants s_c holds
+    int coef_of = -1;   // solve whose class table is loaded
+    unsigned g = 0;     // planes staged by this CTA so far
+    // thread 0 takes units one ahead: `next` is the unit after the current
+    // one (its record is copied to shared memory while the current one
+    // runs), `ahead` the counter value taken for the unit after that
+    int next = 0, ahead = 0;
+    auto fetch = [&](int u, int slot) {
+        if (u < total_units) {
+            cp_async16(smem_addr(&s_rec[slot]), &units[u]);
+            cp_async16(smem_addr(&s_rec[slot]) + 16, reinterpret_cast<const unsigned char *>(&units[u]) + 16);
+        }
+        cp_async_commit();
+    };
+    if (tid == 0) {
+        next = atomicAdd(work_counter, 1);
+        fetch(next, 0);
+        ahead = atomicAdd(work_counter, 1);
+    }
+    for (int i = 0;; i++) {
+        const int slot = i & 1;
         if (tid == 0) {
-            const int u = atomicAdd(work_counter, 1);
-            int lo = 0, hi = nsolves - 1;
-            if (u < total_units) {
-                while (lo < hi) {  // last solve with unit_begin <= u
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (descs[mid].unit_begin <= u)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-            }
+            cp_async_wait<0>();
+            const int u = next;
             s_unit = u;
-            s_solve = lo;
+            // the solve's completed steps, or -1 once it reached its target
+            const int n = u < total_units ? *s_rec[slot].counter : 0;
+            s_n = u < total_units && n < s_rec[slot].steps_target ? n : -1;
+            if (u < total_units) {
+                next = ahead;
+                fetch(next, slot ^ 1);  // read by all threads one unit ago, before the barrier below
+                ahead = next < total_units ? atomicAdd(work_counter, 1) : total_units;
+            }
         }
         __syncthreads();
-        const int u = s_unit, sv = s_solve;
+        const int u = s_unit;
         if (u >= total_units)
             break;
-        const BatchDesc &d = descs[sv];
-        const int n = *d.c[0].step_counter;
-        if (n < d.steps_target) {
+        const BatchUnit rec = s_rec[slot];
+        const BatchDesc &d = descs[rec.solve];
+        const int n = s_n;
+        if (n >= 0) {
             const int par = n & 1;
-            {
-                const int *src = reinterpret_cast<const int *>(&d.c[par]);
-                int *dst = reinterpret_cast<int *>(&s_c);
-                for (int i = tid; i < (int)(sizeof(NativeConsts) / 4); i += G::NTH)
-                    dst[i] = src[i];
-            }
-            if (sv != loaded)
+            const bool consts = rec.solve * 2 + par != loaded, coef = rec.solve != coef_of;
+            if (consts && tid == 0)
+                strip_consts(s_c, d.c[par]);
+            if (coef)
                 strip_load_coef(d.c[par], sm.coef, G::NTH);
-            __syncthreads();
-            loaded = sv;
-            const int local = u - d.unit_begin;
-            const int per_z = d.tiles_x * d.tiles_y;
-            const int bz = local / per_z, rem = local % per_z;
-            const int by = rem / d.tiles_x, bx = rem % d.tiles_x;
-            const unsigned long long ml = memless ? memless[u] : 0ull;
-            if (!strip_unit<RY, W, S, R16>(s_c, d.smaps[par], d.zchunk, bx, by, bz, ml, sm, g, false))
+            if (consts || coef)
+                __syncthreads();
+            loaded = rec.solve * 2 + par;
+            coef_of = rec.solve;
+            if (!strip_unit<RY, W, S, R16>(s_c, d.smaps[par], rec.zchunk, rec.bx, rec.by, rec.bz, rec.memless, sm, g,
+                                           false)) {
+                if (tid == 0)
+                    cp_async_wait<0>();
                 return;
-            g += (unsigned)strip_unit_planes(s_c.nz, d.zchunk, bz);
+            }
+            g += (unsigned)strip_unit_planes(s_c.nz, rec.zchunk, rec.bz);
         }
         __syncthreads();
     }
@@ -112,8 +127,7 @@ struct BatchKernel {
         const int st = opt_in();
         if (st != FDTD_OK)
             return st;
-        fn<<<b.persistent_ctas, 32 * W, smem(b.max_classes), s>>>(b.descs, b.nsolves, b.total_units, b.work_counter,
-                                                                  b.memless);
+        fn<<<b.persistent_ctas, 32 * W, smem(b.max_classes), s>>>(b.descs, b.total_units, b.work_counter, b.units);
         const cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? FDTD_OK : (int)e;
     }

@@ -84,7 +84,8 @@ int scan_material(const uint8_t *mat, int nx, int ny, int nz, int nclasses, unsi
 // for the ez row at z = 0, whose x = 1 neighbour the single-pass kernel does
 // not update.
 constexpr int FUSED_TILE_X = 32;
-__host__ __device__ inline int mur_x_fused_faces(const NativeConsts &c)
+template <class C>
+__host__ __device__ inline int mur_x_fused_faces(const C &c)
 {
     return c.fuse_mur_x && c.mur_x ? (1 | ((c.nx - 1) % FUSED_TILE_X != 0 ? 2 : 0)) : 0;
 }
@@ -164,6 +165,19 @@ struct alignas(64) BatchDesc {
     int pad;
 };
 
+// One work unit of the batched strip kernel, found by its index: the planes
+// of its tile that hold no Debye memory (bit j: plane zc0 + j), its solve's
+// step counter and step target, the solve, the tile (bx, by), the z chunk bz
+// and the chunk length.
+struct alignas(16) BatchUnit {
+    unsigned long long memless;
+    const int *counter;
+    int solve;
+    unsigned short bx, by, bz, zchunk;
+    int steps_target;
+};
+static_assert(sizeof(BatchUnit) == 32, "two 16-byte copies per record");
+
 // One face block of the batched Mur launch: solve, face set, first cell;
 // a block of 256 threads updates BATCH_MUR_CELLS consecutive cells of the set
 // (up to `limit`).
@@ -187,7 +201,7 @@ struct BatchLaunch {
     int r16;          // the compact state holds R in 16 bits (compact is set too)
     int strip;        // compact forms: run by the strip kernel of shape strip_shape
     int strip_shape;
-    const unsigned long long *memless;  // strip kernel: memoryless-plane mask per unit (may be null)
+    const BatchUnit *units;  // strip kernel: one record per unit
 };
 
 // Tensor maps of a single-pass launch over c's buffers (false: not encodable).

@@ -59,9 +59,9 @@ struct StripGeo {
     static constexpr int OFF_R = OFF_H + 3 * pad128(H_BYTES);
     static constexpr int OFF_X = OFF_R + 3 * pad128(R_BYTES);
     static constexpr int OFF_M = OFF_X + pad128(X_BYTES);
-    // x-face tiles: the Mur factors of the tile's rows, near face then far
-    // face ([2][TY] float4)
-    static constexpr int F_BYTES = 2 * TY * 16;
+    // x-face tiles: the Mur factors of the tile's rows ([TY] float4) of its
+    // face (the near one when the tile holds both)
+    static constexpr int F_BYTES = TY * 16;
     static constexpr int OFF_F = pad128(OFF_M + M_BYTES);
     static constexpr int STAGE = pad128(OFF_F + F_BYTES);
     static constexpr unsigned TX_FULL = 3u * E_BYTES + 3u * H_BYTES + 3u * R_BYTES + X_BYTES + M_BYTES;
@@ -150,14 +150,14 @@ __device__ __forceinline__ void fence_async_shared() { asm volatile("fence.proxy
 // factors (the E pass's).
 enum StripIssuePart { ISSUE_ALL = 0, ISSUE_HALO = 1, ISSUE_TILE = 2 };
 
-// A face tile's Mur factors: rows y0 .. of plane 0 of the near and far x face
-// (nullptr: the tile does not hold that face); plane z lies z * plane float4
-// further on.  bytes: the rows inside the grid x 16 (one copy), tx: the bytes
-// of both copies.
+// A face tile's Mur factors: rows y0 .. of plane 0 of its x face (the near
+// one when a tile of a grid at most 32 cells wide holds both; the far face's
+// lanes then read theirs from global memory), nullptr in other tiles; plane z
+// lies z * plane float4 further on.  bytes: the rows inside the grid x 16.
 struct StripFaces {
-    const float4 *near, *far;
+    const float4 *src;
     size_t plane;
-    uint32_t bytes, tx;
+    uint32_t bytes;
 };
 
 template <int RY, int W, bool R16>
@@ -167,7 +167,7 @@ __device__ __forceinline__ void strip_issue(const StripMaps &maps, const StripFa
 {
     using G = StripGeo<RY, W, R16>;
     if (part != ISSUE_TILE) {
-        const unsigned full = (no_r ? G::TX_FULL - 3u * G::R_BYTES - G::X_BYTES : G::TX_FULL) + f.tx;
+        const unsigned full = (no_r ? G::TX_FULL - 3u * G::R_BYTES - G::X_BYTES : G::TX_FULL) + (f.src ? f.bytes : 0u);
         mbar_expect_tx(bar, kind == PLANE_FULL ? full : (kind == PLANE_PRO ? G::TX_PRO : G::TX_EPI));
         if (arm_only)
             return;
@@ -184,10 +184,8 @@ __device__ __forceinline__ void strip_issue(const StripMaps &maps, const StripFa
     if (kind != PLANE_FULL)
         return;
     tma_load_3d(smem_addr(stage + G::OFF_M), &maps.m[9], x0, y0, z, bar);
-    if (f.near)
-        bulk_load(smem_addr(stage + G::OFF_F), f.near + (size_t)z * f.plane, f.bytes, bar);
-    if (f.far)
-        bulk_load(smem_addr(stage + G::OFF_F + G::TY * 16), f.far + (size_t)z * f.plane, f.bytes, bar);
+    if (f.src)
+        bulk_load(smem_addr(stage + G::OFF_F), f.src + (size_t)z * f.plane, f.bytes, bar);
     if (no_r)
         return;
     for (int c = 0; c < 3; c++)
@@ -196,8 +194,54 @@ __device__ __forceinline__ void strip_issue(const StripMaps &maps, const StripFa
         tma_load_3d(smem_addr(stage + G::OFF_X), &maps.m[10], y0, x0 / SX, z, bar);
 }
 
+// The constants the strip unit reads.  The single-solve kernel passes its
+// NativeConsts parameter (constant bank); the batched kernel keeps this
+// smaller copy of the current solve's in shared memory, with the source list
+// left in the descriptor.
+struct StripConsts {
+    int nx, ny, nz;
+    float kx, ky, kz, tx, ty, tz;
+    int scheme, nsources;
+    const int *sources;
+    const DebyeCoef *coef;
+    int nclasses;
+    const float *jz;
+    int njz;
+    int step;
+    int *step_counter;
+    int *err;
+    int fuse_mur_x;
+    const float4 *mur_x;
+};
+
+__device__ __forceinline__ void strip_consts(StripConsts &o, const NativeConsts &c)
+{
+    o.nx = c.nx;
+    o.ny = c.ny;
+    o.nz = c.nz;
+    o.kx = c.kx;
+    o.ky = c.ky;
+    o.kz = c.kz;
+    o.tx = c.tx;
+    o.ty = c.ty;
+    o.tz = c.tz;
+    o.scheme = c.scheme;
+    o.nsources = c.nsources;
+    o.sources = c.sources;
+    o.coef = c.coef;
+    o.nclasses = c.nclasses;
+    o.jz = c.jz;
+    o.njz = c.njz;
+    o.step = c.step;
+    o.step_counter = c.step_counter;
+    o.err = c.err;
+    o.fuse_mur_x = c.fuse_mur_x;
+    o.mur_x = c.mur_x;
+}
+
 // Whether the columns x0..x0+31, rows y0..y0+ty-1, planes zc0..zc1-1 hold a source.
-__device__ __forceinline__ bool strip_has_source(const NativeConsts &c, int x0, int y0, int ty, int zc0, int zc1)
+template <class C>
+__device__ __forceinline__ bool strip_has_source(const C &c, int x0, int y0, int ty, int zc0, int zc1)
 {
     bool any = false;
     for (int s = 0; s < c.nsources; s++) {
@@ -243,7 +287,8 @@ __device__ __forceinline__ void strip_init_bars(const StripSmem &m)
     }
 }
 
-__device__ __forceinline__ void strip_load_coef(const NativeConsts &c, DebyeCoef *coef, int nthreads)
+template <class C>
+__device__ __forceinline__ void strip_load_coef(const C &c, DebyeCoef *coef, int nthreads)
 {
     const float *src = reinterpret_cast<const float *>(c.coef);
     float *dst = reinterpret_cast<float *>(coef);
@@ -257,8 +302,8 @@ __device__ __forceinline__ void strip_load_coef(const NativeConsts &c, DebyeCoef
 // holds no Debye memory.  stall (thread 0 only): leave the second plane's
 // copies unissued (test hook).  Returns false when a bounded wait gave up
 // (the error flag is raised; the CTA must stop).
-template <int RY, int W, int S, bool R16>
-__device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMaps &maps, int zchunk, int bx, int by,
+template <int RY, int W, int S, bool R16, class C>
+__device__ __forceinline__ bool strip_unit(const C &c, const StripMaps &maps, int zchunk, int bx, int by,
                                            int bz, unsigned long long memless, const StripSmem &sm, unsigned g0,
                                            bool stall)
 {
@@ -286,14 +331,11 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
     const bool face_near = (mur_bits & 1) && x0 == 0;
     const bool face_far_cta = (mur_bits & 2) && x0 <= nx - 1 && nx - 1 < x0 + SX;
     const bool face_cta = face_near || face_far_cta;
-    StripFaces faces{nullptr, nullptr, (size_t)ny, 0u, 0u};
+    const bool faces_both = face_near && face_far_cta;
+    StripFaces faces{nullptr, (size_t)ny, 0u};
     if (face_cta) {
         faces.bytes = (uint32_t)min(TY, ny - y0) * 16u;
-        if (face_near)
-            faces.near = c.mur_x + y0;
-        if (face_far_cta)
-            faces.far = c.mur_x + (size_t)nz * ny + y0;
-        faces.tx = (face_near ? faces.bytes : 0u) + (face_far_cta ? faces.bytes : 0u);
+        faces.src = face_near ? c.mur_x + y0 : c.mur_x + (size_t)nz * ny + y0;
     }
     if (tid == 0)
         for (int k = 0; k < S && k < nplanes; k++)
@@ -564,7 +606,9 @@ __device__ __forceinline__ bool strip_unit(const NativeConsts &c, const StripMap
                         const float ey_lo = __shfl_up_sync(all, en1, 1), ez_lo = __shfl_up_sync(all, en2, 1);
                         if (face_lane && y < ny && zmid) {
                             const float4 mf =
-                                reinterpret_cast<const float4 *>(stage(k) + G::OFF_F)[(face_far ? TY : 0) + row];
+                                faces_both && face_far
+                                    ? c.mur_x[((size_t)nz + z) * ny + y]
+                                    : reinterpret_cast<const float4 *>(stage(k) + G::OFF_F)[row];
                             auto mur = [&](float tn, float sn, float sf) {
                                 return __fmul_rn(mf.x, __fsub_rn(__fadd_rn(__fmul_rn(mf.y, tn), __fmul_rn(mf.z, sn)),
                                                                  __fmul_rn(mf.w, sf)));
