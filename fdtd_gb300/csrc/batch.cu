@@ -5,8 +5,9 @@
 // 16-bit form -- and the classes) with
 // rows padded to a multiple of 16 cells, so every solve gets TMA staging, and
 // its own plan (class table, source table, Mur slabs) and step counter.  A
-// batched step is three launches: one persistent kernel over the work units
-// (column tile x z chunk) of all solves, one Mur launch over all solves' face
+// batched step is three launches: one kernel over the work units (column
+// tile x z chunk) of all solves (compact forms: one CTA per unit; D form: a
+// persistent kernel taking units from a counter), one Mur launch over all solves' face
 // cells, and a one-block kernel that advances the step counters.  Step n of a
 // solve uses its counter's parity to pick pointers and tensor maps, so one
 // captured graph serves every step; a solve stops once it reaches its target

@@ -1,12 +1,14 @@
-// batch_strip.cu -- the batched compact forms over column strips: persistent
-// CTAs take work units (column tile x z chunk of some solve) from a counter
-// and run them with the strip kernel's unit (strip_unit.cuh); the ring
-// continues from unit to unit.  The solve's constants come
-// from its descriptor (copied to shared memory), its tensor maps are read by
-// TMA from the descriptor in device memory.  Units of solves that reached
-// their step count are skipped.  The Mur faces and the step counters follow
-// in the batch's other launches (step_fused.cu).  No reference counterpart
-// (the reference runs one grid per process).
+// batch_strip.cu -- the batched compact forms over column strips: one CTA
+// per work unit (column tile x z chunk of some solve), run with the strip
+// kernel's unit (strip_unit.cuh).  A unit's record (built by the host) gives
+// its tile, chunk, solve and memoryless planes; the solve's constants are
+// copied to shared memory, its tensor maps are read by TMA from the
+// descriptor in device memory.  Units of solves that reached their step count
+// exit at once.  The Mur faces and the step counters follow in the batch's
+// other launches (step_fused.cu).  A persistent form (CTAs taking units from
+// an atomic counter, the ring continuing from unit to unit) ran 1.12-1.21x
+// slower on the same work.  No reference counterpart (the reference runs one
+// grid per process).
 #include "per_device.h"
 #include "strip_unit.cuh"
 
@@ -14,82 +16,30 @@ namespace fdtd {
 namespace strip {
 namespace {
 
+// One CTA per work unit (the grid is the batch's work list, taken by the
+// hardware in unit order like the single-solve kernel's grid): the unit's
+// record, its solve's constants in shared memory, then the unit.
 template <int RY, int W, int S, bool R16, int MINB>
 __global__ void __launch_bounds__(32 * W, MINB) batch_strip_kernel(const BatchDesc *__restrict__ descs,
-                                                                   int total_units, int *work_counter,
-                                                                   const BatchUnit *__restrict__ units)
+                                                                  const BatchUnit *__restrict__ units)
 {
     using G = StripGeo<RY, W, R16>;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ StripConsts s_c;
-    __shared__ BatchUnit s_rec[2];  // the current unit's record and the next one's
-    __shared__ int s_unit, s_n;
     const StripSmem sm = strip_smem<RY, W, S, R16>(smem_raw);
+    const BatchUnit rec = units[blockIdx.x];
+    const int n = *rec.counter;
+    if (n >= rec.steps_target)  // the solve is done (uniform over the CTA)
+        return;
     strip_init_bars<S>(sm);
-    const int tid = threadIdx.x;
-    int loaded = -1;    // solve * 2 + parity whose constants s_c holds
-    int coef_of = -1;   // solve whose class table is loaded
-    unsigned g = 0;     // planes staged by this CTA so far
-    // thread 0 takes units one ahead: `next` is the unit after the current
-    // one (its record is copied to shared memory while the current one
-    // runs), `ahead` the counter value taken for the unit after that
-    int next = 0, ahead = 0;
-    auto fetch = [&](int u, int slot) {
-        if (u < total_units) {
-            cp_async16(smem_addr(&s_rec[slot]), &units[u]);
-            cp_async16(smem_addr(&s_rec[slot]) + 16, reinterpret_cast<const unsigned char *>(&units[u]) + 16);
-        }
-        cp_async_commit();
-    };
-    if (tid == 0) {
-        next = atomicAdd(work_counter, 1);
-        fetch(next, 0);
-        ahead = atomicAdd(work_counter, 1);
-    }
-    for (int i = 0;; i++) {
-        const int slot = i & 1;
-        if (tid == 0) {
-            cp_async_wait<0>();
-            const int u = next;
-            s_unit = u;
-            // the solve's completed steps, or -1 once it reached its target
-            const int n = u < total_units ? *s_rec[slot].counter : 0;
-            s_n = u < total_units && n < s_rec[slot].steps_target ? n : -1;
-            if (u < total_units) {
-                next = ahead;
-                fetch(next, slot ^ 1);  // read by all threads one unit ago, before the barrier below
-                ahead = next < total_units ? atomicAdd(work_counter, 1) : total_units;
-            }
-        }
-        __syncthreads();
-        const int u = s_unit;
-        if (u >= total_units)
-            break;
-        const BatchUnit rec = s_rec[slot];
-        const BatchDesc &d = descs[rec.solve];
-        const int n = s_n;
-        if (n >= 0) {
-            const int par = n & 1;
-            const bool consts = rec.solve * 2 + par != loaded, coef = rec.solve != coef_of;
-            if (consts && tid == 0)
-                strip_consts(s_c, d.c[par]);
-            if (coef)
-                strip_load_coef(d.c[par], sm.coef, G::NTH);
-            if (consts || coef)
-                __syncthreads();
-            loaded = rec.solve * 2 + par;
-            coef_of = rec.solve;
-            if (!strip_unit<RY, W, S, R16>(s_c, d.smaps[par], rec.zchunk, rec.bx, rec.by, rec.bz, rec.memless, sm, g,
-                                           false)) {
-                if (tid == 0)
-                    cp_async_wait<0>();
-                return;
-            }
-            g += (unsigned)strip_unit_planes(s_c.nz, rec.zchunk, rec.bz);
-        }
-        __syncthreads();
-    }
-    if (tid == G::STORE_TID)
+    const BatchDesc &d = descs[rec.solve];
+    const int par = n & 1;
+    if (threadIdx.x == 0)
+        strip_consts(s_c, d.c[par]);
+    strip_load_coef(d.c[par], sm.coef, G::NTH);
+    __syncthreads();
+    strip_unit<RY, W, S, R16>(s_c, d.smaps[par], rec.zchunk, rec.bx, rec.by, rec.bz, rec.memless, sm, 0u, false);
+    if (threadIdx.x == G::STORE_TID)
         bulk_wait_all();
 }
 
@@ -127,7 +77,7 @@ struct BatchKernel {
         const int st = opt_in();
         if (st != FDTD_OK)
             return st;
-        fn<<<b.persistent_ctas, 32 * W, smem(b.max_classes), s>>>(b.descs, b.total_units, b.work_counter, b.units);
+        fn<<<b.total_units, 32 * W, smem(b.max_classes), s>>>(b.descs, b.units);
         const cudaError_t e = cudaGetLastError();
         return e == cudaSuccess ? FDTD_OK : (int)e;
     }
