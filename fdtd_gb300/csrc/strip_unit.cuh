@@ -357,6 +357,29 @@ __device__ __forceinline__ bool strip_unit(const C &c, const StripMaps &maps, in
     const bool xy_inside = x0 >= 1 && x0 + SX - 1 <= nx - 2 && y0 >= 1 && y0 + TY - 1 <= ny - 2 && !face_cta &&
                            !unit_src;
 
+    // Range-tested tiles: each component's update range in x and y per row
+    // of the strip (fixed for the unit; the z ranges are per plane).  The
+    // tested path computes every update and keeps it where its range holds.
+    enum : unsigned { M_HX = 1, M_HY = 2, M_HZ = 4, M_E0 = 8, M_E1 = 16, M_E2 = 32, M_EYZ = 64, M_DOM = 128 };
+    unsigned mrow = 0;  // 8 bits per row of the strip
+#pragma unroll
+    for (int r = 0; r < RY; r++) {
+        const int y = y0 + ry0 + r;
+        const bool in_dom = x < nx && y < ny;
+        const bool xi = x >= 1 && x < nx - 1, yi = y >= 1 && y < ny - 1;
+        unsigned m = 0;
+        m |= (xi && y < ny - 1) ? M_HX : 0u;
+        m |= (x < nx - 1 && yi) ? M_HY : 0u;
+        m |= (x < nx - 1 && y < ny - 1) ? M_HZ : 0u;
+        m |= (in_dom && x < nx - 1 && yi) ? M_E0 : 0u;
+        m |= (in_dom && xi && y < ny - 1) ? M_E1 : 0u;
+        m |= (in_dom && xi && yi) ? M_E2 : 0u;
+        m |= (in_dom && x >= 1) ? M_EYZ : 0u;
+        m |= in_dom ? M_DOM : 0u;
+        mrow |= m << (8 * r);
+    }
+    auto has = [&](int r, unsigned bit) { return ((mrow >> (8 * r)) & bit) != 0u; };
+
     float hxm[RY], hym[RY];  // H^{n+1/2} x, y of the strip's cells at z-1
 #pragma unroll
     for (int r = 0; r < RY; r++)
@@ -421,12 +444,12 @@ __device__ __forceinline__ bool strip_unit(const C &c, const StripMaps &maps, in
                 hyn[r] = cm_h(hyn[r], kz, eb(0, er, ec), ex[r], kx, ea(2, er, ec + 1), ez[r]);
                 hzn[r] = cm_h(hzn[r], kx, ea(1, er, ec + 1), ey[r], ky, ex[r + 1], ex[r]);
             } else {
-                if (x >= 1 && x < nx - 1 && y < ny - 1 && zlo)
-                    hxn[r] = cm_h(hxn[r], ky, ez[r + 1], ez[r], ky, eb(1, er, ec), ey[r]);
-                if (x < nx - 1 && y >= 1 && y < ny - 1 && zlo)
-                    hyn[r] = cm_h(hyn[r], kz, eb(0, er, ec), ex[r], kx, ea(2, er, ec + 1), ez[r]);
-                if (x < nx - 1 && y < ny - 1 && zmid)
-                    hzn[r] = cm_h(hzn[r], kx, ea(1, er, ec + 1), ey[r], ky, ex[r + 1], ex[r]);
+                const float vx = cm_h(hxn[r], ky, ez[r + 1], ez[r], ky, eb(1, er, ec), ey[r]);
+                const float vy = cm_h(hyn[r], kz, eb(0, er, ec), ex[r], kx, ea(2, er, ec + 1), ez[r]);
+                const float vz = cm_h(hzn[r], kx, ea(1, er, ec + 1), ey[r], ky, ex[r + 1], ex[r]);
+                hxn[r] = has(r, M_HX) && zlo ? vx : hxn[r];
+                hyn[r] = has(r, M_HY) && zlo ? vy : hyn[r];
+                hzn[r] = has(r, M_HZ) && zmid ? vz : hzn[r];
             }
         }
         if (z < zc0) {  // chunk prologue: only the strip's H x, y at zc0 - 1 are needed
@@ -559,47 +582,35 @@ __device__ __forceinline__ bool strip_unit(const C &c, const StripMaps &maps, in
                         rn2 = cm_r16_rho(kc.a, en2, rn2);
                     }
                 } else {
-                    const bool in_dom = x < nx && y < ny;
-                    const bool xi = x >= 1 && x < nx - 1, yi = y >= 1 && y < ny - 1;
-                    float g0 = 0.0f, g1 = 0.0f, g2 = 0.0f;
-                    if (in_dom && x < nx - 1 && yi && zmid)
-                        g0 = cm_dinc(tcy, hzn[r], hz_ym, tcz, hyn[r], hym[r]);
-                    if (in_dom && xi && y < ny - 1 && zmid)
-                        g1 = cm_dinc(tcz, hxn[r], hxm[r], tcx, hzn[r], hz_xm);
+                    const bool ex_on = has(r, M_E0) && zmid;  // also the range of g0
+                    const float g0 = ex_on ? cm_dinc(tcy, hzn[r], hz_ym, tcz, hyn[r], hym[r]) : 0.0f;
+                    const float g1 =
+                        has(r, M_E1) && zmid ? cm_dinc(tcz, hxn[r], hxm[r], tcx, hzn[r], hz_xm) : 0.0f;
                     bool src = false;
                     if (unit_src)
                         for (int s = 0; s < c.nsources; s++)
                             src |= c.sources[3 * s + 2] == z && c.sources[3 * s] == x && c.sources[3 * s + 1] == y;
-                    if (in_dom && ((xi && yi && zlo) || src)) {
-                        g2 = cm_dinc(tcx, hyn[r], hy_xm, tcy, hxn[r], hx_ym);
-                        if (src)
-                            g2 = __fsub_rn(g2, jz_now);
-                    }
-                    const bool ex_on = in_dom && x < nx - 1 && yi && zmid;
-                    const bool eyz_on = in_dom && x >= 1 && z >= 1;
+                    const float d2 = cm_dinc(tcx, hyn[r], hy_xm, tcy, hxn[r], hx_ym);
+                    const float g2 = has(r, M_DOM) && ((has(r, M_E2) && zlo) || src)
+                                         ? (src ? __fsub_rn(d2, jz_now) : d2)
+                                         : 0.0f;
+                    const bool eyz_on = has(r, M_EYZ) && z >= 1;
                     // not updated: E keeps E^n, R keeps R^n (16-bit R: residual 0)
-                    en0 = ex[r];
-                    en1 = ey[r];
-                    en2 = ez[r];
-                    rn0 = R16 ? 0.0f : r0;
-                    rn1 = R16 ? 0.0f : r1;
-                    rn2 = R16 ? 0.0f : r2;
-                    if (ex_on) {
-                        en0 = cm_e_next(kc, k12, ex[r], g0, r0);
-                        rn0 = cm_r_next(kc, ex[r], g0);
-                        if constexpr (R16)
-                            rn0 = cm_r16_rho(kc.a, en0, rn0);
+                    const float u0 = cm_e_next(kc, k12, ex[r], g0, r0);
+                    const float u1 = cm_e_next(kc, k12, ey[r], g1, r1);
+                    const float u2 = cm_e_next(kc, k12, ez[r], g2, r2);
+                    float s0 = cm_r_next(kc, ex[r], g0), s1 = cm_r_next(kc, ey[r], g1), s2 = cm_r_next(kc, ez[r], g2);
+                    if constexpr (R16) {
+                        s0 = cm_r16_rho(kc.a, u0, s0);
+                        s1 = cm_r16_rho(kc.a, u1, s1);
+                        s2 = cm_r16_rho(kc.a, u2, s2);
                     }
-                    if (eyz_on) {
-                        en1 = cm_e_next(kc, k12, ey[r], g1, r1);
-                        en2 = cm_e_next(kc, k12, ez[r], g2, r2);
-                        rn1 = cm_r_next(kc, ey[r], g1);
-                        rn2 = cm_r_next(kc, ez[r], g2);
-                        if constexpr (R16) {
-                            rn1 = cm_r16_rho(kc.a, en1, rn1);
-                            rn2 = cm_r16_rho(kc.a, en2, rn2);
-                        }
-                    }
+                    en0 = ex_on ? u0 : ex[r];
+                    en1 = eyz_on ? u1 : ey[r];
+                    en2 = eyz_on ? u2 : ez[r];
+                    rn0 = ex_on ? s0 : (R16 ? 0.0f : r0);
+                    rn1 = eyz_on ? s1 : (R16 ? 0.0f : r1);
+                    rn2 = eyz_on ? s2 : (R16 ? 0.0f : r2);
                     if (face_cta) {  // uniform over the CTA: every lane takes part in the shuffles
                         const unsigned all = 0xffffffffu;
                         const float ey_hi = __shfl_down_sync(all, en1, 1), ez_hi = __shfl_down_sync(all, en2, 1);
