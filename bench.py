@@ -104,6 +104,8 @@ def parse_args():
                     help="--impl reference: most seconds of timed CPU steps (fewer steps than --steps if needed)")
     ap.add_argument("--forms-batch-steps", type=int, default=300,
                     help="timed steps of the batched forms in the default run (0: skip them)")
+    ap.add_argument("--no-serve-vs-batch", action="store_true",
+                    help="skip the served loop against the batch on the same 64 solves (forms.serve_vs_batch)")
     ap.add_argument("--forms-serve-seconds", type=float, default=10.0,
                     help="arrival window of the served form in the default run (20 req/s; 0: skip)")
     ap.add_argument("--no-precision", action="store_true",
@@ -509,6 +511,8 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
         binputs = _request_inputs(reqs, Path(btmp.name))
         forms["batch"] = {k: batch_form(k, reqs, binputs, args.warmup, args.forms_batch_steps, True)
                           for k in ("compact", "compact16")}
+        if not args.no_serve_vs_batch:
+            forms["serve_vs_batch"] = serve_vs_batch("compact16", reqs, binputs)
         del binputs
         btmp.cleanup()
     if args.kernel == "single" and not args.no_forms and world == 1 and args.forms_serve_seconds > 0:
@@ -670,6 +674,31 @@ def batch_form(kernel_name: str, reqs, inputs: dict, warmup: int, steps: int, au
            "gpu_launches": 3 * to_run, "clocks": clk.summary()}
     b.close()
     return out
+
+
+def serve_vs_batch(kernel_name: str, reqs, inputs: dict) -> dict:
+    """The served loop against the batch on the same solves, both to the
+    last solve's end: the 64 batch solves arrive at once (the served form at
+    saturation), 25-step chunks, an Ez snapshot every 250 steps; the batch
+    runs them in one batch with no autotuning.  Rates are all cell-updates
+    over the wall time from the first arrival (served) and over the device
+    time of the steps after 3 warm-up steps (batched)."""
+    import fdtd_gb300 as fg
+    from fdtd_gb300 import serve as sv
+
+    batch = batch_form(kernel_name, reqs, inputs, 3, 0, False)
+    reqs0 = [sv.Request(r.rid, 0.0, r.dims, r.frequency, r.steps, r.seed) for r in reqs]
+    with ClockSampler(0) as clk:
+        res = sv.serve(reqs0, budget_bytes=150 * 10 ** 9, chunk=25, snapshot_every=250, scheme=fg.SCHEME_CORRECTED,
+                       inputs=dict(inputs), kernel=KERNELS[kernel_name])
+    summ = res.summary()
+    return {"form": FORM_NAMES[kernel_name], "solves": len(reqs),
+            "batched": {"value": batch["value"], "ms_per_step": batch["ms_per_step"], "steps": batch["steps"],
+                        "clocks": batch["clocks"]},
+            "served": {"value": summ["cell_updates_per_s"], "wall_s": summ["wall_s"],
+                       "gpu_busy_fraction": summ["gpu_busy_fraction"], "completed": summ["completed"],
+                       "p50_ms": summ["p50_ms"], "p99_ms": summ["p99_ms"], "clocks": clk.summary()},
+            "served_over_batched": summ["cell_updates_per_s"] / batch["value"]}
 
 
 def serve_form(kernel_name: str, rate: float, seconds: float, policy: str = "fifo", max_cells: float = 0.0,

@@ -179,7 +179,7 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
           scheme: int = SCHEME_CORRECTED, device: int = 0, clock=time.perf_counter,
           on_snapshot=None, inputs: dict | None = None, kernel: int = KERNEL_SINGLE_PASS,
           policy: str = "fifo", max_active_cells: float | None = None, control: ServeControl | None = None,
-          inflight: int = 2) -> ServeResult:
+          inflight: int = 2, admit_per_turn: int = 4) -> ServeResult:
     """Runs the request stream to completion in real time.  chunk must
     divide snapshot_every so snapshots land on exact step counts.  inputs
     (optional) maps request ids to build_inputs results that arrive with the
@@ -193,7 +193,10 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
     on_snapshot(req, step, plane) receives each snapshot (a copy the callee
     may keep).  control (optional) cancels requests from the host; a request
     whose deadline passes is ended the same way.  inflight: batched chunks
-    queued ahead of the host."""
+    queued ahead of the host.  admit_per_turn: requests admitted per turn of
+    the loop once solves run, so that building and uploading new solves
+    overlaps the queued chunks instead of holding the next chunk back (when
+    nothing runs, one request is admitted and stepped at once)."""
     assert snapshot_every % chunk == 0 and inflight >= 1
     order_queue([], policy)  # rejects an unknown policy before any work
     pending = deque(sorted(requests, key=lambda r: r.arrival))
@@ -257,7 +260,8 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
                 req.status, req.done = "cancelled", req.arrival
             # admit in policy order while the head fits the budget and the cap
             order_queue(queue, policy)
-            while queue:
+            admitted, limit = 0, (admit_per_turn if active else 1)
+            while queue and admitted < limit:
                 req = queue[0]
                 need = batch.need_bytes(*req.dims)
                 if need > budget_bytes:
@@ -283,6 +287,7 @@ def serve(requests: list[Request], budget_bytes: int, chunk: int = 25, snapshot_
                 req.status = "running"
                 active[sid] = [req, 0, src[2], p]
                 active_cells += cells
+                admitted += 1
             if active:
                 # keep at most `inflight` chunks queued: wait for the oldest
                 while len(chunks) >= inflight:
