@@ -119,9 +119,10 @@ int single_shape(bool r16)
     const char *v = std::getenv("FDTD_STRIP_SHAPE");
     if (v && v[0] >= '0' && v[0] < '0' + STRIP_SHAPES && v[1] == 0)
         return v[0] - '0';
-    // measured fastest on the 512 x 512 x 400 phantom: 2 x 4 for 16-bit R,
-    // 1 x 8 for 32-bit R (whose larger stages leave fewer CTAs per SM)
-    return r16 ? 0 : 1;
+    // measured fastest on the 512 x 512 x 400 phantom for both forms: 2 x 4
+    // (32-bit R: 1.021 against 1.025 ms per step for 1 x 8)
+    (void)r16;
+    return 0;
 }
 
 }  // namespace
