@@ -442,8 +442,9 @@ const char *fdtd_solver_kernel_name(const fdtd_solver *s, int k);
 /* ------------------------------------------------------------------------
  * Batch: many independent solves of uneven sizes advanced together (no
  * reference counterpart).  Each solve keeps its own resident state and plan;
- * one batched step is a persistent kernel over the column-tile x z-chunk work
- * units of every solve, one Mur launch over every solve's face cells and a
+ * one batched step is one kernel over the column-tile x z-chunk work units of
+ * every solve (compact forms: one CTA per unit; D form: persistent CTAs taking
+ * units from a counter), one Mur launch over every solve's face cells and a
  * counter advance, replayed as a CUDA graph.  A solve stops at its own step
  * target; adding or removing a solve rebuilds the launch.  Results of a solve
  * are identical whether it runs alone or with others.
