@@ -470,7 +470,7 @@ int fdtd_batch_create_form(int device, int kernel, fdtd_batch **out)
         st = cu(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
     if (st == FDTD_OK) {
         // the batch's own pool keeps freed memory for the next solves
-        // instead of returning it to the driver
+        // instead of handing it back to CUDA
         cudaMemPoolProps props = {};
         props.allocType = cudaMemAllocationTypePinned;
         props.location.type = cudaMemLocationTypeDevice;
