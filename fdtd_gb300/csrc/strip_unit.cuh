@@ -91,13 +91,13 @@ struct StripGeo {
 // (the same shared memory per CTA, 4, 8 or 2 warps), 3 uses 16-row tiles.
 constexpr int STRIP_SHAPES = 4;
 template <int SHAPE> struct Shape;
-// BATCH_CTAS16 / BATCH_CTAS32: resident CTAs per SM the persistent batched
-// kernel is built for, with 16-bit and 32-bit R (its register bound; the
-// solve's constants come from shared memory there, which without a bound
-// costs it 100-160 registers).  Measured on the 64-solve batch: shape 0 runs
-// faster at 6 than at 5 with 16-bit R, and at 5 than at 6 with 32-bit R
-// (where shared memory allows 5); shape 1 spills 136-144 bytes at 5.
-template <> struct Shape<0> { static constexpr int RY = 2, W = 4, BATCH_CTAS16 = 6, BATCH_CTAS32 = 5; };
+// BATCH_CTAS16 / BATCH_CTAS32: resident CTAs per SM the batched kernel is
+// built for, with 16-bit and 32-bit R (its register bound; the solve's
+// constants come from shared memory there).  Measured on the 64-solve batch:
+// shape 0 with 16-bit R runs 2.6 % faster at 5 (no spills) than at 6 (80
+// registers, spills), and with 32-bit R shared memory allows 5; shape 1
+// spills 136-144 bytes at 5.
+template <> struct Shape<0> { static constexpr int RY = 2, W = 4, BATCH_CTAS16 = 5, BATCH_CTAS32 = 5; };
 template <> struct Shape<1> { static constexpr int RY = 1, W = 8, BATCH_CTAS16 = 4, BATCH_CTAS32 = 4; };
 template <> struct Shape<2> { static constexpr int RY = 4, W = 2, BATCH_CTAS16 = 8, BATCH_CTAS32 = 8; };
 template <> struct Shape<3> { static constexpr int RY = 4, W = 4, BATCH_CTAS16 = 2, BATCH_CTAS32 = 2; };
