@@ -331,7 +331,8 @@ class Solver:
         self.material = np.ascontiguousarray(material, np.uint8)
         specs = np.ascontiguousarray(specs, np.float32).reshape(-1, 4)
         if nclasses is None:
-            nclasses = int(self.material.max()) + 1
+            # every row given; the library keeps those up to the largest class present
+            nclasses = min(len(specs), MAX_CLASSES)
         self.specs = np.ascontiguousarray(specs[:nclasses])
         cfg = SolverConfig(params=C.pointer(p.raw), material=self.material.ctypes.data_as(C.POINTER(C.c_uint8)),
                            specs=fptr(self.specs), nclasses=nclasses, scheme=scheme, kernel=kernel, device=device)
@@ -361,8 +362,13 @@ class Solver:
     def stream(self) -> int:
         return lib().fdtd_solver_stream(self.handle) or 0
 
-    def field(self, name: str) -> np.ndarray:
-        out = np.empty(self.params.shape, np.float32)
+    def field(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """One field volume (nz, ny, nx) float32; into `out` when given (a
+        reused buffer skips the first-touch cost of fresh host pages)."""
+        if out is None:
+            out = np.empty(self.params.shape, np.float32)
+        elif out.shape != self.params.shape or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError(f"out must be a C-contiguous float32 array of shape {self.params.shape}")
         check(lib().fdtd_solver_get_field(self.handle, FIELD_ID[name], fptr(out)), "fdtd_solver_get_field")
         return out
 
@@ -491,7 +497,7 @@ class Batch:
         material = np.ascontiguousarray(material, np.uint8)
         specs = np.ascontiguousarray(specs, np.float32).reshape(-1, 4)
         if nclasses is None:
-            nclasses = int(material.max()) + 1
+            nclasses = min(len(specs), MAX_CLASSES)
         specs = np.ascontiguousarray(specs[:nclasses])
         cfg = SolverConfig(params=C.pointer(p.raw), material=material.ctypes.data_as(C.POINTER(C.c_uint8)),
                            specs=fptr(specs), nclasses=nclasses, scheme=scheme, kernel=0, device=0)

@@ -559,8 +559,12 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
     int st = cu(cudaSetDevice(b->device));
     if (st != FDTD_OK)
         return st;
-    if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, nullptr) != FDTD_OK)
+    if (cfg->nclasses < 1 || cfg->nclasses > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
+    int top = 0;
+    if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, nullptr, &top) != FDTD_OK)
+        return FDTD_ERR_INVALID;
+    const int ncls = top + 1;  // the classes up to the largest one present
     auto *v = new (std::nothrow) BatchSolve();
     if (!v)
         return FDTD_ERR_NOMEM;
@@ -570,7 +574,7 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
     v->steps_target = steps;
     // everything of the new solve goes on the side stream: the batch stream
     // keeps running the steps already queued
-    st = plan_create_on(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, b->pool, b->side, &v->plan);
+    st = plan_create_on(p, cfg->specs, ncls, cfg->scheme, nullptr, b->pool, b->side, &v->plan);
     const size_t fbytes = (v->ncell * sizeof(float) + 255) & ~size_t(255);
     const size_t total = state_bytes(p->nx, p->ny, p->nz, b->compact, b->r16);
     const size_t dbytes = b->r16 ? r16_array_bytes(v->ncell) : fbytes;
@@ -616,7 +620,7 @@ int fdtd_batch_add(fdtd_batch *b, const fdtd_solver_config *cfg, int steps, int 
         return st;
     }
     if (b->compact)
-        v->memless8 = strip_plane_flags(cfg->material, p->nx, p->ny, p->nz, p->nx, cfg->specs, cfg->nclasses);
+        v->memless8 = strip_plane_flags(cfg->material, p->nx, p->ny, p->nz, p->nx, cfg->specs, ncls);
     v->bytes = total + plan_bytes(p->nx, p->ny, p->nz);
     v->id = b->next_id++;
     b->solves.push_back(v);

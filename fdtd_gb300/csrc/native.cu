@@ -37,33 +37,59 @@ DebyeCoef debye_coef(float dt, float eps0, float sigma, float eps_s, float eps_i
     return k;
 }
 
-int scan_material(const uint8_t *mat, int nx, int ny, int nz, int nclasses, unsigned long long *hash)
+int scan_material(const uint8_t *mat, int nx, int ny, int nz, int nclasses, unsigned long long *hash, int *top_class)
 {
-    // per z plane, in parallel: the largest class and an FNV-1a hash; the
-    // plane hashes are then folded in order by FNV-1a over their bytes
+    // Per z plane, in parallel: the largest class, and a fingerprint made of
+    // four FNV-1a chains over the plane's little-endian 64-bit words (word i
+    // feeds chain i % 4, so the four multiplies overlap), its tail bytes fed
+    // to chain 0.  The chains, then the plane fingerprints, are folded in
+    // order by FNV-1a over their bytes.
+    constexpr unsigned long long FNV_BASIS = 1469598103934665603ULL, FNV_PRIME = 1099511628211ULL;
+    auto fold = [](unsigned long long h, unsigned long long v) {
+        for (int b = 0; b < 8; b++)
+            h = (h ^ ((v >> (8 * b)) & 0xffu)) * FNV_PRIME;
+        return h;
+    };
     const size_t plane = (size_t)nx * ny;
     std::vector<unsigned long long> ph(nz);
     std::vector<int> top(nz, 0);
     parallel_for(nz, 0, [&](int z) {
         const uint8_t *q = mat + (size_t)z * plane;
-        unsigned long long h = 1469598103934665603ULL;
-        int m = 0;
-        for (size_t i = 0; i < plane; i++) {
-            m = q[i] > m ? q[i] : m;
-            h = (h ^ q[i]) * 1099511628211ULL;
+        unsigned long long lane[4] = {FNV_BASIS, FNV_BASIS ^ 1, FNV_BASIS ^ 2, FNV_BASIS ^ 3};
+        const size_t quads = plane / 32;
+        for (size_t i = 0; i < quads; i++) {
+            unsigned long long w[4];
+            std::memcpy(w, q + 32 * i, sizeof w);
+            for (int l = 0; l < 4; l++) {
+#if defined(__BYTE_ORDER__) && __BYTE_ORDER__ == __ORDER_BIG_ENDIAN__
+                w[l] = __builtin_bswap64(w[l]);  // little-endian words on every host
+#endif
+                lane[l] = (lane[l] ^ w[l]) * FNV_PRIME;
+            }
         }
+        for (size_t i = 32 * quads; i < plane; i++)
+            lane[0] = (lane[0] ^ q[i]) * FNV_PRIME;
+        unsigned long long h = FNV_BASIS;
+        for (int l = 0; l < 4; l++)
+            h = fold(h, lane[l]);
         ph[z] = h;
+        uint8_t m = 0;  // a max reduction the compiler vectorises
+        for (size_t i = 0; i < plane; i++)
+            m = q[i] > m ? q[i] : m;
         top[z] = m;
     });
-    unsigned long long h = 1469598103934665603ULL;
+    unsigned long long h = FNV_BASIS;
+    int m = 0;
     for (int z = 0; z < nz; z++) {
         if (top[z] >= nclasses)
             return FDTD_ERR_INVALID;
-        for (int b = 0; b < 8; b++)
-            h = (h ^ ((ph[z] >> (8 * b)) & 0xffu)) * 1099511628211ULL;
+        m = std::max(m, top[z]);
+        h = fold(h, ph[z]);
     }
     if (hash)
         *hash = h;
+    if (top_class)
+        *top_class = m;
     return FDTD_OK;
 }
 
@@ -448,16 +474,23 @@ int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int sc
         const float me = p->mu0 * p->eps0, dt = p->dt, h = p->dx;
         for (int face = 0; face < 2; face++) {
             const float *slab = rp[face ? 3 : 0].data();
+            float last_self = 0.0f, last_nbr = 0.0f;
+            float4 v{};
+            bool have = false;  // v holds the factors of (last_self, last_nbr)
             for (int z = 0; z < p->nz; z++)
                 for (int y = 0; y < p->ny; y++) {
                     const size_t b = ((size_t)z * p->ny + y) * 2;
                     const float r_self = slab[b + (face ? 1 : 0)], r_nbr = slab[b + (face ? 0 : 1)];
-                    const float q_self = h * std::sqrt(me * r_self), q_nbr = h * std::sqrt(me * r_nbr);
-                    float4 v;
-                    v.x = 1.0f / (dt + q_self);
-                    v.y = dt - q_nbr;
-                    v.z = dt + q_nbr;
-                    v.w = dt - q_self;
+                    if (!have || r_self != last_self || r_nbr != last_nbr) {
+                        const float q_self = h * std::sqrt(me * r_self), q_nbr = h * std::sqrt(me * r_nbr);
+                        v.x = 1.0f / (dt + q_self);
+                        v.y = dt - q_nbr;
+                        v.z = dt + q_nbr;
+                        v.w = dt - q_self;
+                        last_self = r_self;
+                        last_nbr = r_nbr;
+                        have = true;
+                    }
                     murx[((size_t)face * p->nz + z) * p->ny + y] = v;
                 }
         }

@@ -75,8 +75,10 @@ struct NativeConsts {
 NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n);
 
 // Checks every class index of a dense volume against nclasses (host threads
-// over z planes) and, if hash is not null, returns a hash of the volume.
-int scan_material(const uint8_t *mat, int nx, int ny, int nz, int nclasses, unsigned long long *hash);
+// over z planes); returns, where the pointers are not null, a hash of the
+// volume and its largest class index.
+int scan_material(const uint8_t *mat, int nx, int ny, int nz, int nclasses, unsigned long long *hash,
+                  int *top_class = nullptr);
 
 // x-face Mur updates done by the single-pass kernel: bit 0 the x = 0 face,
 // bit 1 the x = nx-1 face (only when x = nx-2 lies in the same 32-column

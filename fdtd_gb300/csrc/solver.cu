@@ -314,10 +314,7 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     if (st != FDTD_OK)
         return st;
     const size_t n = (size_t)p->nx * p->ny * p->nz;
-    if (p->nx < 3 || p->ny < 3 || p->nz < 3)
-        return FDTD_ERR_INVALID;
-    unsigned long long mhash = 0;
-    if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, &mhash) != FDTD_OK)
+    if (p->nx < 3 || p->ny < 3 || p->nz < 3 || cfg->nclasses < 1 || cfg->nclasses > FDTD_MAX_CLASSES)
         return FDTD_ERR_INVALID;
     auto *s = new (std::nothrow) fdtd_solver();
     if (!s)
@@ -327,14 +324,6 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     s->ncell = n;
     s->kernel = cfg->kernel;
     s->scheme = cfg->scheme;
-    s->nclasses = cfg->nclasses;
-    s->specs.assign(cfg->specs, cfg->specs + 4 * (size_t)cfg->nclasses);
-    s->material_hash = mhash;  // checkpoints must come from the same class volume
-    st = fdtd_plan_create(p, cfg->specs, cfg->nclasses, cfg->scheme, nullptr, &s->plan);
-    if (st != FDTD_OK) {
-        delete s;
-        return st;
-    }
     // H: two buffers for the single-pass kernels, one for the two-pass pair;
     // E: two slots; D: two slots, or one R array for the compact form (FP16
     // residuals and their scale words for the 16-bit form)
@@ -382,10 +371,26 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         st = cu(cudaMemsetAsync(s->d_block, 0, total, s->stream));
     if (st == FDTD_OK)
         st = cu(cudaMemcpyAsync(s->mat, cfg->material, n, cudaMemcpyHostToDevice, s->stream));
+    // the class volume is checked and the plan built while the device clears
+    // the state and takes the volume
+    unsigned long long mhash = 0;
+    int top = 0;
+    if (st == FDTD_OK &&
+        scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, &mhash, &top) != FDTD_OK)
+        st = FDTD_ERR_INVALID;
+    // the classes up to the largest one present: the kernels stage that many
+    // table entries
+    const int ncls = top + 1;
+    if (st == FDTD_OK) {
+        s->nclasses = ncls;
+        s->specs.assign(cfg->specs, cfg->specs + 4 * (size_t)ncls);
+        s->material_hash = mhash;  // checkpoints must come from the same class volume
+        st = fdtd_plan_create(p, cfg->specs, ncls, cfg->scheme, nullptr, &s->plan);
+    }
     if (st == FDTD_OK && stores_no_d(cfg->kernel)) {
         // tile-planes without Debye memory: the strip kernel skips their R
         const std::vector<unsigned char> flags =
-            strip_plane_flags(cfg->material, p->nx, p->ny, p->nz, p->nx, cfg->specs, cfg->nclasses);
+            strip_plane_flags(cfg->material, p->nx, p->ny, p->nz, p->nx, cfg->specs, ncls);
         s->memless_rows = strip_shape_rows(strip_single_shape(cfg->kernel == FDTD_KERNEL_COMPACT_R16));
         const int zchunk = strip_zchunk(p->nz);
         std::vector<unsigned long long> masks((size_t)((p->nz + zchunk - 1) / zchunk) *

@@ -326,7 +326,9 @@ typedef struct fdtd_solver_config {
     const FdtdParams *params;   /* grid, constants, sources, optional jz */
     const uint8_t *material;    /* host: nx*ny*nz class indices */
     const float *specs;         /* host: nclasses x 4 (sigma, eps_s, eps_i, tau) */
-    int nclasses;
+    int nclasses;               /* rows of specs, 1 .. FDTD_MAX_CLASSES; every class index
+                                   must be below it.  The solve keeps the rows up to the
+                                   largest class present in the material. */
     int scheme;                 /* FDTD_SCHEME_* */
     int kernel;                 /* FDTD_KERNEL_* */
     int device;                 /* CUDA device ordinal */

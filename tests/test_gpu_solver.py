@@ -216,3 +216,35 @@ def test_drop_in_compact16_binary_output_equals_the_solver(cuda, tmp_path):
     ez = s.field("ez")
     s.close()
     assert np.array_equal(got.view(np.uint32), ez.view(np.uint32))
+
+
+@pytest.mark.parametrize("kernel", [fg.KERNEL_SINGLE_PASS, fg.KERNEL_COMPACT_R16])
+def test_class_rows_beyond_the_material_change_nothing(cuda, tmp_path, kernel):
+    """The solve keeps the specs rows up to the largest class present: every
+    row of the table given, or just the two the sphere uses, same bits; a
+    class index at or above the rows given is refused."""
+    path = ph.c1_inputs(tmp_path, n=20, t_max=30)
+    p = fg.Params.read(path)
+    codes = fg.load_material_codes(p, tmp_path / "pgm")
+    specs = fg.read_specs(tmp_path / "mat_specs")
+    assert len(specs) == fg.MAX_CLASSES and codes.max() == 1
+    out = {}
+    for rows in (2, None):
+        with fg.Solver(p, codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel, nclasses=rows) as s:
+            s.run(25)
+            out[rows] = s.fields()
+    for name in out[2]:
+        assert np.array_equal(out[2][name], out[None][name]), name
+    with pytest.raises(fg.FdtdError):
+        fg.Solver(p, codes, specs, scheme=fg.SCHEME_CORRECTED, kernel=kernel, nclasses=1)
+
+
+def test_field_into_a_caller_buffer(cuda, tmp_path):
+    p, codes, specs, s = solver_from_files(tmp_path, 20, 30, fg.KERNEL_SINGLE_PASS)
+    s.run(12)
+    buf = np.full(p.shape, np.nan, np.float32)
+    assert s.field("ez", out=buf) is buf
+    assert np.array_equal(buf, s.field("ez"))
+    with pytest.raises(ValueError):
+        s.field("ez", out=np.empty(p.shape, np.float64))
+    s.close()
