@@ -65,6 +65,14 @@ __device__ __forceinline__ float mur_value(float dt, float h, float me, float rp
     return __fmul_rn(__fdiv_rn(1.0f, __fadd_rn(dt, q_self)), num);
 }
 
+// mur_value of a face cell whose slab layers hold one value, from that
+// value's factors k = (1/(dt+q), dt-q, dt+q, dt-q): the same operations on
+// the same operands, so the same bits.
+__device__ __forceinline__ float mur_value_k(float4 k, float t_nbr, float s_nbr, float s_self)
+{
+    return __fmul_rn(k.x, __fsub_rn(__fadd_rn(__fmul_rn(k.y, t_nbr), __fmul_rn(k.z, s_nbr)), __fmul_rn(k.w, s_self)));
+}
+
 // The twelve (component, face) sets that updateMurBoundary writes.  For face
 // set f, (len_u, len_v) is the extent and (u0, v0) the first coordinate of
 // its two in-face axes; `axis` is the face normal (0 x, 1 y, 2 z) and `far`
@@ -201,12 +209,14 @@ struct MurSet {
 // ... below v_end: all loads are issued before any store, so K independent loads per
 // array are in flight per thread (face cells are written, their neighbours
 // and E^n are only read, so no cell is both).
-template <int K>
+// UNI: the set's slab holds one value whose factors are kf (no slab loads,
+// no square roots or division).
+template <int K, bool UNI = false>
 __device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride, int v_end, int nx, int ny, int nz,
                                             int pitch,
                                             float dt, float hx, float hy, float hz, float me, const MurSlabs &rp,
                                             float *t0, float *t1, float *t2, const float *s0, const float *s1,
-                                            const float *s2, bool fix_ey)
+                                            const float *s2, bool fix_ey, float4 kf = float4{})
 {
     const MurSet ms(f, nx, ny, nz, hx, hy, hz, rp, t0, t1, t2, s0, s1, s2, fix_ey);
     const MurFace &m = ms.m;
@@ -214,6 +224,8 @@ __device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride,
         return;
     const int u = m.u0 + iu;
     float rs[K], rn[K], tn[K], sn[K], sf[K];
+    (void)rs;
+    (void)rn;
     size_t face[K];
     bool on[K];
 #pragma unroll
@@ -223,8 +235,10 @@ __device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride,
         const MurCellIdx c = mur_cell_idx(m, u, m.v0 + (on[k] ? iv : 0), nx, ny, nz, pitch);
         face[k] = c.face;
         if (on[k]) {
-            rs[k] = ms.slab[c.rs];
-            rn[k] = ms.slab[c.rn];
+            if constexpr (!UNI) {
+                rs[k] = ms.slab[c.rs];
+                rn[k] = ms.slab[c.rn];
+            }
             tn[k] = ms.TN[c.nbr];
             sn[k] = ms.S[c.nbr];
             sf[k] = ms.S[c.face];
@@ -232,19 +246,23 @@ __device__ __forceinline__ void mur_apply_k(int f, int iu, int iv0, int vstride,
     }
 #pragma unroll
     for (int k = 0; k < K; k++)
-        if (on[k])
-            ms.T[face[k]] = mur_value(dt, ms.h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
+        if (on[k]) {
+            if constexpr (UNI)
+                ms.T[face[k]] = mur_value_k(kf, tn[k], sn[k], sf[k]);
+            else
+                ms.T[face[k]] = mur_value(dt, ms.h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
+        }
 }
 
 // mur_apply for K cells of one face set at flat in-face indices idx0,
 // idx0 + stride, ... (row-major over (v, u), below len_u * len_v < 2^31);
 // loads before stores as in mur_apply_k.
-template <int K>
+template <int K, bool UNI = false>
 __device__ __forceinline__ void mur_apply_flat_k(int f, unsigned idx0, unsigned stride, int nx, int ny, int nz,
                                                  int pitch, float dt, float hx, float hy, float hz, float me,
                                                  const MurSlabs &rp, float *t0, float *t1, float *t2,
                                                  const float *s0, const float *s1, const float *s2, bool fix_ey,
-                                                 unsigned limit = 0)
+                                                 unsigned limit = 0, float4 kf = float4{})
 {
     const MurSet ms(f, nx, ny, nz, hx, hy, hz, rp, t0, t1, t2, s0, s1, s2, fix_ey);
     const MurFace &m = ms.m;
@@ -265,8 +283,10 @@ __device__ __forceinline__ void mur_apply_flat_k(int f, unsigned idx0, unsigned 
         const MurCellIdx c = mur_cell_idx(m, m.u0 + (int)(i % lu), m.v0 + (int)(i / lu), nx, ny, nz, pitch);
         face[k] = c.face;
         if (on[k]) {
-            rs[k] = ms.slab[c.rs];
-            rn[k] = ms.slab[c.rn];
+            if constexpr (!UNI) {
+                rs[k] = ms.slab[c.rs];
+                rn[k] = ms.slab[c.rn];
+            }
             tn[k] = ms.TN[c.nbr];
             sn[k] = ms.S[c.nbr];
             sf[k] = ms.S[c.face];
@@ -274,8 +294,12 @@ __device__ __forceinline__ void mur_apply_flat_k(int f, unsigned idx0, unsigned 
     }
 #pragma unroll
     for (int k = 0; k < K; k++)
-        if (on[k])
-            ms.T[face[k]] = mur_value(dt, ms.h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
+        if (on[k]) {
+            if constexpr (UNI)
+                ms.T[face[k]] = mur_value_k(kf, tn[k], sn[k], sf[k]);
+            else
+                ms.T[face[k]] = mur_value(dt, ms.h, me, rs[k], rn[k], tn[k], sn[k], sf[k]);
+        }
 }
 
 }  // namespace fdtd

@@ -122,6 +122,10 @@ NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n)
     c.njz = p->njz;
     c.rp = p->rp;
     c.mur_x = p->d_mur_x;
+    for (int k = 0; k < 6; k++)
+        for (int j = 0; j < 4; j++)
+            c.mur_k[k][j] = p->mur_k[k][j];
+    c.mur_uniform = p->mur_uniform;
     c.step = n;
     c.step_counter = nullptr;
     c.err = p->d_err;
@@ -277,6 +281,21 @@ __global__ void __launch_bounds__(MUR_THREADS) native_mur_kernel(NativeConsts c)
         len_v = 1;   // ez: only the z = 0 row is left
     }
     const bool fix = c.scheme == FDTD_SCHEME_CORRECTED;
+    const int slab = m.axis + 3 * m.far;
+    if ((c.mur_uniform >> slab) & 1) {
+        // one value in the set's slab: its factors, picked by constant indices
+        // (a run-time index into the argument block would copy it to local memory)
+        float4 kf = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int s = 0; s < 6; s++)
+            if (s == slab)
+                kf = make_float4(c.mur_k[s][0], c.mur_k[s][1], c.mur_k[s][2], c.mur_k[s][3]);
+        for (int iv = blockIdx.y; iv < len_v; iv += MUR_ROWS * gridDim.y)
+            mur_apply_k<MUR_ROWS, true>(f, iu, iv, gridDim.y, len_v, c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz,
+                                        c.me, c.rp, c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1],
+                                        c.e_cur[2], fix, kf);
+        return;
+    }
     for (int iv = blockIdx.y; iv < len_v; iv += MUR_ROWS * gridDim.y)
         mur_apply_k<MUR_ROWS>(f, iu, iv, gridDim.y, len_v, c.nx, c.ny, c.nz, c.pitch, c.dt, c.hx, c.hy, c.hz, c.me, c.rp,
                               c.e_prev[0], c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2], fix);
@@ -425,6 +444,30 @@ int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int sc
     } else {
         fdtd_setup_mur_uniform(p, p->defaultSigma, p->defaultEpsS, p->defaultEpsI, p->defaultTauD, rp[0].data(),
                                rp[1].data(), rp[2].data(), rp[3].data(), rp[4].data(), rp[5].data());
+    }
+
+    // slabs that hold one value: their factors once, rounded one operation at
+    // a time as mur_value rounds them (IEEE single, no contraction)
+    {
+        const float me = p->mu0 * p->eps0, dt = p->dt;
+        const float hs[3] = {p->dx, p->dy, p->dz};
+        for (int k = 0; k < 6; k++) {
+            const float v = rp[k][0];
+            bool one = true;
+            for (float r : rp[k])
+                if (!(r == v)) {
+                    one = false;
+                    break;
+                }
+            if (!one)
+                continue;
+            const float q = hs[k % 3] * std::sqrt(me * v);
+            plan->mur_k[k][0] = 1.0f / (dt + q);
+            plan->mur_k[k][1] = dt - q;
+            plan->mur_k[k][2] = dt + q;
+            plan->mur_k[k][3] = dt - q;
+            plan->mur_uniform |= 1 << k;
+        }
     }
 
     size_t total = 0;

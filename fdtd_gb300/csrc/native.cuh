@@ -22,6 +22,8 @@ struct fdtd_plan {
     float *d_jz = nullptr;                // FDTD_JZ_LEN entries
     fdtd::MurSlabs rp{};                  // six Mur slabs
     float4 *d_mur_x = nullptr;            // x-face Mur coefficients, [face][z][y] (see mur_x_coef)
+    float mur_k[6][4] = {};               // per Mur slab holding one value: the factors of every cell
+    int mur_uniform = 0;                  // bit s: slab s (NativeConsts::mur_k order) holds one value
     int *d_err = nullptr;                 // device error flag
     int *d_stall = nullptr;               // test hook word (NativeConsts::stall_once)
     bool pooled = false;                  // d_block comes from a stream-ordered pool (plan_create_on)
@@ -70,6 +72,14 @@ struct NativeConsts {
     // relaxation (R stays +0 there: not loaded, not stored); may be null
     const unsigned long long *memless;
     int memless_rows;      // tile rows the masks were made for (other tile heights ignore them)
+    // Mur slabs that hold one value (slab s: x0, y0, z0, x_end, y_end, z_end,
+    // i.e. face normal s % 3, far face s / 3; set when every entry of both
+    // layers of the slab is that value, as for slabs made from the default
+    // material): bit s of mur_uniform, and the factors 1/(dt+q), dt-q, dt+q,
+    // dt-q of its every face cell, q = h sqrt(me rp), each rounded as
+    // mur_value rounds it
+    float mur_k[6][4];
+    int mur_uniform;
 };
 
 NativeConsts make_consts(const fdtd_plan *p, const fdtd_native_fields *f, int n);

@@ -742,6 +742,16 @@ __global__ void __launch_bounds__(256) batch_mur_kernel(const BatchDesc *__restr
     const NativeConsts &c = d.c[n & 1];
     // BATCH_MUR_CELLS cells from b.first: thread t takes first + t + k * 256
     // (faces of batched solves hold < 2^31 cells)
+    const MurFace m = mur_face(b.face, c.nx, c.ny, c.nz);
+    const int slab = m.axis + 3 * m.far;
+    if ((c.mur_uniform >> slab) & 1) {  // one value in the set's slab: its factors
+        const float4 kf = make_float4(c.mur_k[slab][0], c.mur_k[slab][1], c.mur_k[slab][2], c.mur_k[slab][3]);
+        mur_apply_flat_k<BATCH_MUR_CELLS / 256, true>(b.face, (unsigned)b.first + threadIdx.x, 256u, c.nx, c.ny, c.nz,
+                                                      c.pitch, c.dt, c.hx, c.hy, c.hz, c.me, c.rp, c.e_prev[0],
+                                                      c.e_prev[1], c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
+                                                      c.scheme == FDTD_SCHEME_CORRECTED, (unsigned)b.limit, kf);
+        return;
+    }
     mur_apply_flat_k<BATCH_MUR_CELLS / 256>(b.face, (unsigned)b.first + threadIdx.x, 256u, c.nx, c.ny, c.nz, c.pitch,
                                             c.dt, c.hx, c.hy, c.hz, c.me, c.rp, c.e_prev[0], c.e_prev[1],
                                             c.e_prev[2], c.e_cur[0], c.e_cur[1], c.e_cur[2],
