@@ -307,6 +307,24 @@ int launch_status()
     return e == cudaSuccess ? FDTD_OK : (int)e;
 }
 
+// n copies of v from dst on (slabs and face factors that hold one value).
+template <class T>
+__global__ void __launch_bounds__(256) fill_kernel(T *__restrict__ dst, size_t n, T v)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = v;
+}
+
+template <class T>
+cudaError_t fill_on(T *dst, size_t n, T v, cudaStream_t stream)
+{
+    if (n == 0)
+        return cudaSuccess;
+    const unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 1024);
+    fill_kernel<T><<<blocks, 256, 0, stream>>>(dst, n, v);
+    return cudaGetLastError();
+}
+
 bool fields_ok(const fdtd_native_fields *f, bool need_h_out)
 {
     if (!f)
@@ -427,41 +445,50 @@ int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int sc
     plan->njz = FDTD_JZ_LEN;
 
     // Mur slabs (from the default material when not given, as the reference
-    // computes them before loadMaterials, fdtd.cu:59,65)
+    // computes them before loadMaterials, fdtd.cu:59,65).  A slab whose
+    // entries are all one value (every slab made from the default material)
+    // is filled on the device and never built on the host.
     const size_t nrp[6] = {2 * (size_t)p->ny * p->nz, (size_t)p->nx * 2 * p->nz, (size_t)p->nx * p->ny * 2,
                            2 * (size_t)p->ny * p->nz, (size_t)p->nx * 2 * p->nz, (size_t)p->nx * p->ny * 2};
-    std::vector<std::vector<float>> rp(6);
-    for (int k = 0; k < 6; k++)
-        rp[k].resize(nrp[k]);
+    float one_value[6] = {};
+    bool one[6] = {};
     if (rp_host) {
         for (int k = 0; k < 6; k++) {
             if (!rp_host[k]) {
                 delete plan;
                 return FDTD_ERR_INVALID;
             }
-            std::copy(rp_host[k], rp_host[k] + nrp[k], rp[k].begin());
+            // one value: every entry with the first one's bits (and not a NaN)
+            const float v = rp_host[k][0];
+            uint32_t vb;
+            std::memcpy(&vb, &v, sizeof vb);
+            one[k] = v == v;
+            for (size_t i = 0; i < nrp[k] && one[k]; i++) {
+                uint32_t b;
+                std::memcpy(&b, rp_host[k] + i, sizeof b);
+                one[k] = b == vb;
+            }
+            one_value[k] = v;
         }
     } else {
-        fdtd_setup_mur_uniform(p, p->defaultSigma, p->defaultEpsS, p->defaultEpsI, p->defaultTauD, rp[0].data(),
-                               rp[1].data(), rp[2].data(), rp[3].data(), rp[4].data(), rp[5].data());
+        // fdtd_setup_mur_uniform's two values: x slabs, y and z slabs
+        const float vx = mur_rp_value(p, p->defaultSigma, p->defaultEpsS, p->defaultEpsI, p->defaultTauD, false);
+        const float vyz = mur_rp_value(p, p->defaultSigma, p->defaultEpsS, p->defaultEpsI, p->defaultTauD, true);
+        for (int k = 0; k < 6; k++) {
+            one[k] = true;
+            one_value[k] = k % 3 == 0 ? vx : vyz;
+        }
     }
 
-    // slabs that hold one value: their factors once, rounded one operation at
-    // a time as mur_value rounds them (IEEE single, no contraction)
+    // one-valued slabs: their factors once, rounded one operation at a time
+    // as mur_value rounds them (IEEE single, no contraction)
     {
         const float me = p->mu0 * p->eps0, dt = p->dt;
         const float hs[3] = {p->dx, p->dy, p->dz};
         for (int k = 0; k < 6; k++) {
-            const float v = rp[k][0];
-            bool one = true;
-            for (float r : rp[k])
-                if (!(r == v)) {
-                    one = false;
-                    break;
-                }
-            if (!one)
+            if (!one[k])
                 continue;
-            const float q = hs[k % 3] * std::sqrt(me * v);
+            const float q = hs[k % 3] * std::sqrt(me * one_value[k]);
             plan->mur_k[k][0] = 1.0f / (dt + q);
             plan->mur_k[k][1] = dt - q;
             plan->mur_k[k][2] = dt + q;
@@ -493,11 +520,10 @@ int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int sc
     }
     plan->d_block = base;
     plan->pooled = pool != nullptr;
-    // copies: blocking ones, or (pool) ones ordered on the stream that the
-    // caller synchronises before the host vectors below go away
+    // Copies and fills are ordered on `stream` (null: the legacy default
+    // stream), which is synchronised before the host vectors below go away.
     auto put = [&](void *dst, const void *src, size_t n) {
-        return pool ? cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, stream)
-                    : cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
+        return cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, stream);
     };
     plan->d_coef = reinterpret_cast<DebyeCoef *>(base + offs[0]);
     plan->d_jz = reinterpret_cast<float *>(base + offs[1]);
@@ -508,15 +534,26 @@ int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int sc
     plan->d_err = reinterpret_cast<int *>(base + err_off);
     plan->d_stall = plan->d_err + 1;
     plan->d_mur_x = reinterpret_cast<float4 *>(base + murx_off);
+    std::vector<float4> murx;
     {
         // The x-face Mur factors of mur_value, rounded one operation at a time
         // in the same order (IEEE single: sqrt and division correctly rounded,
         // no contraction), so the kernel that applies them gets the bits the
-        // Mur kernel gets from the slabs.
-        std::vector<float4> murx(nmurx);
+        // Mur kernel gets from the slabs.  A one-valued x slab gives one
+        // factor set for its whole face (its mur_k row).
         const float me = p->mu0 * p->eps0, dt = p->dt, h = p->dx;
-        for (int face = 0; face < 2; face++) {
-            const float *slab = rp[face ? 3 : 0].data();
+        const size_t per_face = (size_t)p->nz * p->ny;
+        for (int face = 0; face < 2 && e == cudaSuccess; face++) {
+            const int k = face ? 3 : 0;
+            float4 *dst = plan->d_mur_x + face * per_face;
+            if (one[k]) {
+                e = fill_on(dst, per_face, make_float4(plan->mur_k[k][0], plan->mur_k[k][1], plan->mur_k[k][2],
+                                                       plan->mur_k[k][3]), stream);
+                continue;
+            }
+            if (murx.empty())
+                murx.resize(nmurx);
+            const float *slab = rp_host[k];
             float last_self = 0.0f, last_nbr = 0.0f;
             float4 v{};
             bool have = false;  // v holds the factors of (last_self, last_nbr)
@@ -534,20 +571,20 @@ int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int sc
                         last_nbr = r_nbr;
                         have = true;
                     }
-                    murx[((size_t)face * p->nz + z) * p->ny + y] = v;
+                    murx[(size_t)face * per_face + (size_t)z * p->ny + y] = v;
                 }
+            e = put(dst, murx.data() + face * per_face, sizeof(float4) * per_face);
         }
-        e = put(plan->d_mur_x, murx.data(), sizeof(float4) * nmurx);
         if (e == cudaSuccess)  // error flag, test hook word
-            e = pool ? cudaMemsetAsync(plan->d_err, 0, 2 * sizeof(int), stream)
-                     : cudaMemset(plan->d_err, 0, 2 * sizeof(int));
+            e = cudaMemsetAsync(plan->d_err, 0, 2 * sizeof(int), stream);
         if (e == cudaSuccess)
             e = put(plan->d_coef, coef.data(), sizeof(DebyeCoef) * FDTD_MAX_CLASSES);
         if (e == cudaSuccess)
             e = put(plan->d_jz, jz.data(), sizeof(float) * FDTD_JZ_LEN);
         for (int k = 0; k < 6 && e == cudaSuccess; k++)
-            e = put(rpd[k], rp[k].data(), sizeof(float) * nrp[k]);
-        if (pool && e == cudaSuccess)
+            e = one[k] ? fill_on(rpd[k], nrp[k], one_value[k], stream)
+                       : put(rpd[k], rp_host[k], sizeof(float) * nrp[k]);
+        if (e == cudaSuccess)
             e = cudaStreamSynchronize(stream);  // the host vectors are released below
     }
     if (e != cudaSuccess) {
