@@ -489,7 +489,10 @@ def run_gb300_arm(args, rank: int, local_rank: int, world: int, dist) -> None:
         t1 = time.perf_counter()
         replicas.barrier(dist)
         assert len(got) == args.steps and final.shape == (nz, ny, nx)
-        h2d = codes.nbytes + 4 * (len(specs) * 8 + 65536 + 2 * (2 * ny * nz + 2 * nx * nz + 2 * nx * ny))
+        # copied from the host: the class volume, the plan's 256-entry class
+        # table (32 B each) and its 65536-entry source table; the Mur slabs
+        # of the default material are filled on the device
+        h2d = codes.nbytes + 256 * 32 + 4 * 65536
         d2h = plane_bytes * args.steps + final.nbytes
         e_cells, e_t = replicas.aggregate(cells * args.steps, t1 - t0, dist, device=f"cuda:{local_rank}")
         e2e = {"value": e_cells / e_t, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d / args.steps,
