@@ -395,18 +395,24 @@ int fdtd_plan_create(const FdtdParams *p, const float *specs, int nclasses, int 
 
 namespace fdtd {
 
-int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int scheme, const float *const rp_host[6],
-                   cudaMemPool_t pool, cudaStream_t stream, fdtd_plan **out)
+int plan_params_check(const FdtdParams *p, int scheme)
 {
-    if (!p || !specs || !out || nclasses < 1 || nclasses > FDTD_MAX_CLASSES || p->nx < 3 || p->ny < 3 ||
-        p->nz < 3 || p->nz > 65535 || p->sourcesCount < 0 || p->sourcesCount > FDTD_MAX_SOURCES ||
-        (scheme != FDTD_SCHEME_REFERENCE && scheme != FDTD_SCHEME_CORRECTED))
+    if (!p || p->nx < 3 || p->ny < 3 || p->nz < 3 || p->nz > 65535 || p->sourcesCount < 0 ||
+        p->sourcesCount > FDTD_MAX_SOURCES || (scheme != FDTD_SCHEME_REFERENCE && scheme != FDTD_SCHEME_CORRECTED))
         return FDTD_ERR_INVALID;
     for (int s = 0; s < p->sourcesCount; s++) {
         const int *q = p->sources + 3 * s;
         if (q[0] < 1 || q[0] >= p->nx || q[1] < 1 || q[1] >= p->ny || q[2] < 0 || q[2] >= p->nz)
             return FDTD_ERR_INVALID;
     }
+    return FDTD_OK;
+}
+
+int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int scheme, const float *const rp_host[6],
+                   cudaMemPool_t pool, cudaStream_t stream, fdtd_plan **out)
+{
+    if (!specs || !out || nclasses < 1 || nclasses > FDTD_MAX_CLASSES || plan_params_check(p, scheme) != FDTD_OK)
+        return FDTD_ERR_INVALID;
     fdtd_plan *plan = new (std::nothrow) fdtd_plan();
     if (!plan)
         return FDTD_ERR_NOMEM;

@@ -257,9 +257,14 @@ int launch_strip_compact16(const NativeConsts &c, cudaStream_t s);
 // Reads and clears the plan's device error flag (FDTD_ERR_DEVICE_TIMEOUT if set).
 int plan_error(const fdtd_plan *p);
 
+// The checks fdtd_plan_create makes of the parameters and the scheme
+// (grid of at least 3 cells per axis and at most 65535 planes, sources inside
+// the grid): FDTD_OK or FDTD_ERR_INVALID, before any allocation.
+int plan_params_check(const FdtdParams *p, int scheme);
+
 // fdtd_plan_create with the plan's device memory taken from pool in stream
-// order on stream (copies on that stream, which is synchronised before the
-// call returns); with a null pool, as fdtd_plan_create.  plan_destroy_on
+// order on stream (copies and fills on that stream, which is synchronised
+// before the call returns); with a null pool and stream, as fdtd_plan_create.  plan_destroy_on
 // frees a pooled plan in stream order on stream (no device-wide wait), any
 // other plan as fdtd_plan_destroy does.
 int plan_create_on(const FdtdParams *p, const float *specs, int nclasses, int scheme, const float *const rp_host[6],

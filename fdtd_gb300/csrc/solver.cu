@@ -314,8 +314,8 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     if (st != FDTD_OK)
         return st;
     const size_t n = (size_t)p->nx * p->ny * p->nz;
-    if (p->nx < 3 || p->ny < 3 || p->nz < 3 || cfg->nclasses < 1 || cfg->nclasses > FDTD_MAX_CLASSES)
-        return FDTD_ERR_INVALID;
+    if (cfg->nclasses < 1 || cfg->nclasses > FDTD_MAX_CLASSES || plan_params_check(p, cfg->scheme) != FDTD_OK)
+        return FDTD_ERR_INVALID;  // before any allocation
     auto *s = new (std::nothrow) fdtd_solver();
     if (!s)
         return FDTD_ERR_NOMEM;
