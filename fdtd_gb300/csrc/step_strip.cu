@@ -52,8 +52,10 @@ __global__ void __launch_bounds__(32 * W) strip_step_kernel(const __grid_constan
 
 // ------------------------------------------------------------------ host side
 
-// z chunks of at most 24 planes: measured fastest for both storage forms on
-// the 512 x 512 x 400 phantom (12, 16, 24, 32, 48 tried)
+// z chunks of at most 24 planes, for both storage forms: on the
+// 512 x 512 x 400 phantom within 0.5 % of the fastest limit in every sweep
+// (12, 16, 20, 22, 23, 25, 27, 29, 32, 48 tried; in the latest, 23 and 29
+// ran 0.4 % and 0.2 % faster, 25 0.7 % and 20 1.2 % slower)
 #ifndef FDTD_STRIP_ZCHUNK
 #define FDTD_STRIP_ZCHUNK 24
 #endif
