@@ -5,6 +5,8 @@ import re
 import subprocess
 from pathlib import Path
 
+import numpy as np
+
 import fdtd_gb300 as fg
 
 HEADER_DIR = Path(__file__).resolve().parent.parent / "include"
@@ -44,6 +46,33 @@ def test_invalid_arguments_return_status_without_a_gpu():
     assert L.fdtd_plan_create(None, None, 0, 0, None, None) == fg.FDTD_ERR_INVALID
     assert L.fdtd_solver_create(None, None) == fg.FDTD_ERR_INVALID
     assert L.fdtd_step(None, None, 0, None) == fg.FDTD_ERR_INVALID
+
+
+def test_plan_parameters_checked_before_any_device_call():
+    """fdtd_plan_create refuses a bad grid, source, scheme or class count
+    with FDTD_ERR_INVALID before it touches the device (so without a GPU)."""
+    import ctypes as C
+
+    L = fg.lib()
+    specs = np.zeros((2, 4), np.float32)
+    specs[:, 1:3] = 1.0
+    src = (C.c_int * 3)(5, 5, 5)
+
+    def params(nx=16, ny=16, nz=16, sources=(5, 5, 5)):
+        raw = fg.FdtdParams()
+        raw.nx, raw.ny, raw.nz = nx, ny, nz
+        src[:] = sources
+        raw.sourcesCount, raw.sources = 1, C.cast(src, C.POINTER(C.c_int))
+        raw.dt, raw.dx, raw.dy, raw.dz, raw.mu0, raw.eps0 = 1.9e-12, 1e-3, 1e-3, 1e-3, 1.2566371e-06, 8.85e-12
+        return raw
+
+    h = C.c_void_p()
+    sp = specs.ctypes.data_as(C.POINTER(C.c_float))
+    for raw, ncls, scheme in [(params(nx=2), 2, 0), (params(nz=70000), 2, 0), (params(sources=(0, 5, 5)), 2, 0),
+                              (params(sources=(5, 16, 5)), 2, 0), (params(sources=(5, 5, 16)), 2, 0),
+                              (params(), 2, 7), (params(), 0, 0), (params(), fg.MAX_CLASSES + 1, 0)]:
+        assert L.fdtd_plan_create(C.byref(raw), sp, ncls, scheme, None, C.byref(h)) == fg.FDTD_ERR_INVALID
+        assert not h.value
 
 
 def test_drop_in_executable_built_and_reports_usage():
