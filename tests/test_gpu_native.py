@@ -41,6 +41,27 @@ def test_native_matches_fp32_oracle_reference_scheme(cuda, dims, seed, mode):
 
 
 @pytest.mark.parametrize("mode", ["single", "two_pass"])
+def test_native_mixed_one_valued_and_varying_mur_slabs(cuda, mode):
+    """A slab whose entries are all one value takes the Mur kernel's
+    constant-factor path (and, for an x slab, a factor table filled on the
+    device), any other slab the slab path: three of each, against the FP32
+    oracle on the same slabs."""
+    dims = (40, 24, 18)
+    nx, ny, nz = dims
+    codes, specs, rp, sources, consts, jz = random_case(nx, ny, nz, 11, nsrc=2)
+    for k in (0, 2, 4):  # x = 0, z = 0 and y = ny-1 slabs one-valued
+        rp[k] = np.full_like(rp[k], rp[k].flat[0])
+    steps = 14
+    media = class_media(codes, specs, rp)
+    st = po.State(nx, ny, nz, np.float32)
+    po.run(po.make_cfg(dims, jz, sources=sources, consts=consts), media, st, 0, steps)
+    want = st.latest(steps)
+    raw = make_params(dims, consts, sources, jz)
+    got = run_native(cuda, raw, specs, codes, rp, steps, mode=mode)
+    assert_fields_close(got, want)
+
+
+@pytest.mark.parametrize("mode", ["single", "two_pass"])
 def test_native_corrected_scheme_matches_fp64_oracle(cuda, mode):
     dims = (41, 23, 19)
     nx, ny, nz = dims
