@@ -324,6 +324,27 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
     s->ncell = n;
     s->kernel = cfg->kernel;
     s->scheme = cfg->scheme;
+    // The host scan of the class volume, then the plan, run on a helper
+    // thread while this one allocates the state, has the device clear it and
+    // uploads the volume.
+    unsigned long long mhash = 0;
+    int top = 0, helper_st = FDTD_OK;
+    fdtd_plan *plan = nullptr;
+    auto scan_and_plan = [&] {
+        if (scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, &mhash, &top) != FDTD_OK) {
+            helper_st = FDTD_ERR_INVALID;
+            return;
+        }
+        helper_st = cu(cudaSetDevice(cfg->device));  // the current device is per thread
+        if (helper_st == FDTD_OK)  // the classes up to the largest one present
+            helper_st = fdtd_plan_create(p, cfg->specs, top + 1, cfg->scheme, nullptr, &plan);
+    };
+    std::thread helper;
+    try {
+        helper = std::thread(scan_and_plan);
+    } catch (...) {
+        scan_and_plan();  // no thread to be had: the same work in line
+    }
     // H: two buffers for the single-pass kernels, one for the two-pass pair;
     // E: two slots; D: two slots, or one R array for the compact form (FP16
     // residuals and their scale words for the 16-bit form)
@@ -371,13 +392,11 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         st = cu(cudaMemsetAsync(s->d_block, 0, total, s->stream));
     if (st == FDTD_OK)
         st = cu(cudaMemcpyAsync(s->mat, cfg->material, n, cudaMemcpyHostToDevice, s->stream));
-    // the class volume is checked and the plan built while the device clears
-    // the state and takes the volume
-    unsigned long long mhash = 0;
-    int top = 0;
-    if (st == FDTD_OK &&
-        scan_material(cfg->material, p->nx, p->ny, p->nz, cfg->nclasses, &mhash, &top) != FDTD_OK)
-        st = FDTD_ERR_INVALID;
+    if (helper.joinable())
+        helper.join();
+    s->plan = plan;  // destroyed with the solver on any failure below
+    if (st == FDTD_OK)
+        st = helper_st;
     // the classes up to the largest one present: the kernels stage that many
     // table entries
     const int ncls = top + 1;
@@ -385,7 +404,6 @@ int fdtd_solver_create(const fdtd_solver_config *cfg, fdtd_solver **out)
         s->nclasses = ncls;
         s->specs.assign(cfg->specs, cfg->specs + 4 * (size_t)ncls);
         s->material_hash = mhash;  // checkpoints must come from the same class volume
-        st = fdtd_plan_create(p, cfg->specs, ncls, cfg->scheme, nullptr, &s->plan);
     }
     if (st == FDTD_OK && stores_no_d(cfg->kernel)) {
         // tile-planes without Debye memory: the strip kernel skips their R
