@@ -92,3 +92,15 @@ def test_kernel_form_ids_match_the_header():
     assert ids == {"FDTD_KERNEL_SINGLE_PASS": fg.KERNEL_SINGLE_PASS, "FDTD_KERNEL_TWO_PASS": fg.KERNEL_TWO_PASS,
                    "FDTD_KERNEL_COMPACT": fg.KERNEL_COMPACT, "FDTD_KERNEL_COMPACT_R16": fg.KERNEL_COMPACT_R16}
     assert set(fg.COMPACT_KERNELS) == {fg.KERNEL_COMPACT, fg.KERNEL_COMPACT_R16}
+
+
+def test_field_output_buffer_checked_before_the_library_call():
+    """Solver.field(name, out=...) refuses a buffer of the wrong shape, type or
+    layout before it calls the library (host logic; no solver is created)."""
+    s = fg.Solver.__new__(fg.Solver)  # only the attributes field() reads first
+    s.params = type("P", (), {"shape": (4, 5, 6)})()
+    s.handle = None
+    for bad in (np.empty((4, 5, 7), np.float32), np.empty((4, 5, 6), np.float64),
+                np.empty((6, 5, 4), np.float32).transpose(2, 1, 0)):
+        with np.testing.assert_raises(ValueError):
+            s.field("ez", out=bad)
